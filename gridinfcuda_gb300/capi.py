@@ -1,0 +1,252 @@
+"""ctypes binding of the C ABI (include/ginf_gb300.h) for numpy and torch buffers.
+
+Host buffers are numpy arrays (or CPU tensors); device buffers are CUDA torch
+tensors.  All buffers of one call must live in the same memory kind.  Every
+function raises :class:`GinfError` on a non-zero ``ginf_status``.  The shared
+library is loaded from the package directory; when it has not been built the
+first call raises instead of computing anything elsewhere.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import synth
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libginf_gb300.so")
+
+# Enumerations (values as in include/ginf_gb300.h).
+OK, ERR_INVALID_ARGUMENT, ERR_UNSUPPORTED, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_TIMEOUT, ERR_NO_DEVICE = range(7)
+F32, I32, F64 = 0, 1, 2
+HOST, DEVICE = 0, 1
+RULE_REFERENCE, RULE_STANDARD = 0, 1
+STORE_NATIVE, STORE_F16 = 0, 1
+DECODE_STALE, DECODE_FRESH = 0, 1
+NORM_MEAN, NORM_MIN = 0, 1
+EXPLICIT, POTTS, TRUNC_LINEAR, TRUNC_QUAD = synth.EXPLICIT, synth.POTTS, synth.TRUNC_LINEAR, synth.TRUNC_QUAD
+
+_i32 = ctypes.c_int32
+_p = ctypes.c_void_p
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [("width", _i32), ("height", _i32), ("num_labels", _i32), ("cost_type", _i32),
+                ("sm_model", _i32), ("memory", _i32), ("data_costs", _p), ("sm_costs", _p)]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("msg_rule", _i32), ("msg_store", _i32), ("decode", _i32), ("normalize", _i32),
+                ("compute_type", _i32), ("tile_nodes", _i32), ("stages", _i32), ("reserved0", _i32),
+                ("stream", _p), ("msgs_out", _p), ("reserved", ctypes.c_int64 * 6)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("total_ms", "upload_ms", "prepare_ms", "sweep_ms", "level0_sweep_ms",
+                                               "icm_ms", "energy_ms", "download_ms")] + \
+               [(n, ctypes.c_int64) for n in ("kernel_launches", "level0_sweep_launches", "node_label_iters",
+                                              "h2d_bytes", "d2h_bytes")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class GinfError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"ginf status {status}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def lib():
+    """The loaded libginf_gb300.so (raises if it was never built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with gridinfcuda_gb300.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        L.ginf_version.restype = ctypes.c_char_p
+        L.ginf_last_error.restype = ctypes.c_char_p
+        L.ginf_default_options.argtypes = [ctypes.POINTER(Options)]
+        L.ginf_workspace_create.argtypes = [ctypes.POINTER(_p)]
+        L.ginf_workspace_destroy.argtypes = [_p]
+        L.ginf_decode_hbp.argtypes = [_p, ctypes.POINTER(Grid), _i32, _i32, _p, ctypes.POINTER(Options),
+                                      ctypes.POINTER(Stats)]
+        L.ginf_decode_icm.argtypes = [_p, ctypes.POINTER(Grid), _p, _i32, _i32, _p, ctypes.POINTER(Options),
+                                      ctypes.POINTER(Stats)]
+        L.ginf_energy.argtypes = [_p, ctypes.POINTER(Grid), _p, ctypes.POINTER(ctypes.c_double),
+                                  ctypes.POINTER(Options)]
+        L.ginf_solve.argtypes = [_p, ctypes.POINTER(Grid), _i32, _i32, _i32, _p, ctypes.POINTER(ctypes.c_double),
+                                 ctypes.POINTER(Options), ctypes.POINTER(Stats)]
+        L.ginf_stereo_costs.argtypes = [_i32, _i32, _i32, _i32, _p, _p, ctypes.c_float, ctypes.c_float, _p, _p]
+        for name in ("ginf_decode_hbp", "ginf_decode_icm", "ginf_energy", "ginf_solve", "ginf_stereo_costs",
+                     "ginf_workspace_create", "ginf_workspace_destroy"):
+            getattr(L, name).restype = _i32
+        _lib = L
+    return _lib
+
+
+def check(status: int):
+    if status != OK:
+        raise GinfError(status, lib().ginf_last_error().decode())
+
+
+class Workspace:
+    """Reusable device buffers (``ginf_workspace``); use one per thread."""
+
+    def __init__(self):
+        h = _p()
+        check(lib().ginf_workspace_create(ctypes.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            lib().ginf_workspace_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _is_torch(a):
+    return type(a).__module__.startswith("torch")
+
+
+def _ptr(a):
+    """(address, memory kind) of a numpy array or torch tensor."""
+    if a is None:
+        return None, None
+    if _is_torch(a):
+        if not a.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return a.data_ptr(), (DEVICE if a.is_cuda else HOST)
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return a.ctypes.data, HOST
+
+
+def _dtype_code(a):
+    name = str(a.dtype)
+    if name.endswith("float32"):
+        return F32
+    if name.endswith("int32"):
+        return I32
+    raise ValueError(f"costs must be float32 or int32, got {a.dtype}")
+
+
+def make_grid(D, V, model):
+    """ginf_grid for label-planar costs D (L, H, W) and a flat L*L table V."""
+    L, H, W = D.shape
+    dp, dm = _ptr(D)
+    vp, vm = _ptr(V)
+    if dm != vm:
+        raise ValueError("D and V must live in the same memory kind")
+    if V.shape[-1] * (V.shape[0] if len(V.shape) == 2 else 1) != L * L:
+        raise ValueError("V must hold L*L entries")
+    return Grid(W, H, L, _dtype_code(D), int(model), dm, dp, vp)
+
+
+def options(rule=RULE_REFERENCE, store=STORE_NATIVE, decode=DECODE_STALE, normalize=NORM_MEAN, compute_type=-1,
+            tile_nodes=0, stages=0, stream=None, msgs_out=None):
+    o = Options()
+    lib().ginf_default_options(ctypes.byref(o))
+    o.msg_rule, o.msg_store, o.decode, o.normalize = rule, store, decode, normalize
+    o.compute_type, o.tile_nodes, o.stages = compute_type, tile_nodes, stages
+    o.stream = stream if stream is not None else None
+    o.msgs_out = msgs_out
+    return o
+
+
+def _new_like(D, shape, dtype):
+    if _is_torch(D):
+        import torch
+        tdt = {np.int32: torch.int32, np.float32: torch.float32, np.float64: torch.float64}[dtype]
+        return torch.zeros(shape, dtype=tdt, device=D.device)
+    return np.zeros(shape, dtype=dtype)
+
+
+def _msg_dtype(D, compute_type):
+    ct = _dtype_code(D) if compute_type < 0 else compute_type
+    return {F32: np.float32, I32: np.int32, F64: np.float64}[ct]
+
+
+def decode_hbp(D, V, model, levels, iters, labels=None, *, workspace=None, want_msgs=False, want_stats=False,
+               **opt):
+    """Hierarchical (levels > 1) or loopy BP; returns labels [, msgs] [, stats]."""
+    L, H, W = D.shape
+    g = make_grid(D, V, model)
+    lab = labels if labels is not None else _new_like(D, (H, W), np.int32)
+    msgs = _new_like(D, (H, W, 4, L), _msg_dtype(D, opt.get("compute_type", -1))) if want_msgs else None
+    o = options(msgs_out=_ptr(msgs)[0] if msgs is not None else None, **opt)
+    st = Stats()
+    ws = workspace.handle if workspace is not None else None
+    check(lib().ginf_decode_hbp(ws, ctypes.byref(g), levels, iters, _ptr(lab)[0], ctypes.byref(o),
+                                ctypes.byref(st) if want_stats else None))
+    out = [lab]
+    if want_msgs:
+        out.append(msgs)
+    if want_stats:
+        out.append(st.as_dict())
+    return out[0] if len(out) == 1 else tuple(out)
+
+
+def decode_icm(D, V, model, initial, iters, asynchronous=False, *, workspace=None, want_stats=False, **opt):
+    L, H, W = D.shape
+    g = make_grid(D, V, model)
+    res = _new_like(D, (H, W), np.int32)
+    o = options(**opt)
+    st = Stats()
+    ws = workspace.handle if workspace is not None else None
+    check(lib().ginf_decode_icm(ws, ctypes.byref(g), _ptr(initial)[0], iters, int(asynchronous), _ptr(res)[0],
+                                ctypes.byref(o), ctypes.byref(st) if want_stats else None))
+    return (res, st.as_dict()) if want_stats else res
+
+
+def energy(D, V, model, labels, *, workspace=None):
+    g = make_grid(D, V, model)
+    e = ctypes.c_double()
+    ws = workspace.handle if workspace is not None else None
+    check(lib().ginf_energy(ws, ctypes.byref(g), _ptr(labels)[0], ctypes.byref(e), None))
+    return e.value
+
+
+def solve(D, V, model, levels, iters, icm_iters, labels=None, *, workspace=None, want_stats=False, **opt):
+    """HBP + Jacobi ICM + FP64 energy in one call; returns (labels, energy[, stats])."""
+    L, H, W = D.shape
+    g = make_grid(D, V, model)
+    lab = labels if labels is not None else _new_like(D, (H, W), np.int32)
+    o = options(**opt)
+    st = Stats()
+    e = ctypes.c_double()
+    ws = workspace.handle if workspace is not None else None
+    check(lib().ginf_solve(ws, ctypes.byref(g), levels, iters, icm_iters, _ptr(lab)[0], ctypes.byref(e),
+                           ctypes.byref(o), ctypes.byref(st) if want_stats else None))
+    return (lab, e.value, st.as_dict()) if want_stats else (lab, e.value)
+
+
+def stereo_costs(left, right, L, coef, cap, out, stream=None):
+    """Device cost volume (L, H, W) float32 into the CUDA tensor ``out``."""
+    H, W = left.shape
+    lp, lm = _ptr(left)
+    rp, _ = _ptr(right)
+    op, om = _ptr(out)
+    if om != DEVICE:
+        raise ValueError("out must be a CUDA tensor")
+    check(lib().ginf_stereo_costs(W, H, L, lm, lp, rp, coef, cap, op, stream))
+    return out
+
+
+def version() -> str:
+    return lib().ginf_version().decode()

@@ -1,0 +1,469 @@
+// aux_kernels.cu -- every kernel of the inference path other than the
+// half-sweep: cost layout transform, HBP pyramid, coarse-to-fine message
+// initialisation, label fills, fresh-belief decode, message export, ICM
+// (Jacobi and exact Gauss-Seidel wavefront), FP64 energy, stereo costs.
+#include <cuda_fp16.h>
+
+#include "ginf_internal.h"
+
+namespace ginf_gpu {
+
+namespace {
+
+__device__ __forceinline__ int ddx(int d) { return d == 1 ? 1 : (d == 3 ? -1 : 0); }  // utils.h:36
+__device__ __forceinline__ int ddy(int d) { return d == 0 ? 1 : (d == 2 ? -1 : 0); }  // utils.h:37
+
+__device__ __forceinline__ bool on_border(int x, int y, int W, int H) {
+    return x == 0 || y == 0 || x == W - 1 || y == H - 1;
+}
+
+template <typename M>
+__device__ __forceinline__ double msg_to_double(M v) {
+    return (double)v;
+}
+template <>
+__device__ __forceinline__ double msg_to_double<__half>(__half v) {
+    return (double)__half2float(v);
+}
+
+constexpr int kThreads = 256;
+
+inline unsigned blocks_for(size_t n, int per_block = kThreads) { return (unsigned)((n + per_block - 1) / per_block); }
+
+// ---------------------------------------------------------------------------
+// Label-planar costs (x + W*y + W*H*l, the reference's Matrix(3,W,H,L)) into
+// the D part of level-0 records.  One block transposes 32 nodes x Lp labels
+// through shared memory (stride 33 avoids bank conflicts); reads are
+// coalesced along x, writes along l.  Labels L..Lp-1 are zero-filled.
+template <typename Tin, typename T>
+__global__ void k_costs_to_records(const Tin *__restrict__ src, int W, int H, int L, int Lp,
+                                   unsigned char *__restrict__ rec, uint32_t rec_bytes) {
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    T *tile = reinterpret_cast<T *>(sm_raw);
+    const int x0 = blockIdx.x * 32, y = blockIdx.y;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    for (int l = ty; l < Lp; l += 8) {
+        const int x = x0 + tx;
+        T v = T(0);
+        if (l < L && x < W) v = (T)src[(size_t)x + (size_t)W * y + (size_t)W * H * l];
+        tile[l * 33 + tx] = v;
+    }
+    __syncthreads();
+    const int nn = min(32, W - x0);
+    for (int idx = ty * 32 + tx; idx < nn * Lp; idx += 256) {
+        const int i = idx / Lp, l = idx - i * Lp;
+        T *d = reinterpret_cast<T *>(rec + ((size_t)y * W + x0 + i) * rec_bytes);
+        d[l] = tile[l * 33 + i];
+    }
+}
+
+// HBP pyramid, bp.cc:100-117: D_t(X,Y) = sum of the (up to) four finer nodes,
+// accumulated from zero in the finer level's raster order.
+template <typename T>
+__global__ void k_pyramid(const unsigned char *__restrict__ frec, int fW, int fH, unsigned char *__restrict__ crec,
+                          int cW, int cH, int L, int Lp, uint32_t rec_bytes) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t total = (size_t)cW * cH * Lp;
+    if (idx >= total) return;
+    const size_t node = idx / Lp;
+    const int l = (int)(idx - node * Lp);
+    const int X = (int)(node % cW), Y = (int)(node / cW);
+    T acc = T(0);
+    if (l < L) {
+        for (int dy = 0; dy < 2; ++dy) {
+            const int y = 2 * Y + dy;
+            if (y >= fH) break;
+            for (int dx = 0; dx < 2; ++dx) {
+                const int x = 2 * X + dx;
+                if (x >= fW) break;
+                acc += reinterpret_cast<const T *>(frec + ((size_t)y * fW + x) * rec_bytes)[l];
+            }
+        }
+    }
+    reinterpret_cast<T *>(crec + node * rec_bytes)[l] = acc;
+}
+
+// Materialised message initialisation of a level (used when a level runs
+// fewer than two half-sweeps, so the fused first sweep cannot stand in).
+// Reference: msgs_t(x,y,d) = msgs_{t+1}(x/2,y/2,d), stored at the sender
+// (bp.cc:129-139).  In the receiver layout the slot in_t(p,d) carries the
+// message of q = p + dir(d), i.e. msgs_{t+1}(q/2, OPP(d)), which sits at the
+// coarse receiver R = q/2 - dir(d) in slot d.  Border senders (at either
+// level) never update, so their messages are zero.  crec == nullptr zeroes
+// every slot (the top level).
+__global__ void k_init_messages(unsigned char *__restrict__ rec, int W, int H, const unsigned char *__restrict__ crec,
+                                int cW, int cH, uint32_t rec_bytes, uint32_t d_bytes, uint32_t m_bytes) {
+    const uint32_t chunks = m_bytes / 16;
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t total = (size_t)W * H * 4 * chunks;
+    if (idx >= total) return;
+    const uint32_t c = (uint32_t)(idx % chunks);
+    const int d = (int)((idx / chunks) % 4);
+    const size_t node = idx / (chunks * 4);
+    const int x = (int)(node % W), y = (int)(node / W);
+    uint4 v = make_uint4(0, 0, 0, 0);
+    const int qx = x + ddx(d), qy = y + ddy(d);
+    if (crec && qx >= 0 && qy >= 0 && qx < W && qy < H && !on_border(qx, qy, W, H)) {
+        const int Qx = qx >> 1, Qy = qy >> 1;
+        if (!on_border(Qx, Qy, cW, cH)) {
+            const int Rx = Qx - ddx(d), Ry = Qy - ddy(d);
+            v = *reinterpret_cast<const uint4 *>(crec + ((size_t)Ry * cW + Rx) * rec_bytes + d_bytes + d * m_bytes +
+                                                 16 * c);
+        }
+    }
+    *reinterpret_cast<uint4 *>(rec + node * rec_bytes + d_bytes + d * m_bytes + 16 * c) = v;
+}
+
+__global__ void k_fill_interior(int32_t *labels, int W, int H, int32_t value) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t n = (size_t)(W - 2) * (H - 2);
+    if (idx >= n) return;
+    const int x = 1 + (int)(idx % (W - 2)), y = 1 + (int)(idx / (W - 2));
+    labels[(size_t)y * W + x] = value;
+}
+
+// Fresh beliefs from the final messages (GINF_DECODE_FRESH): argmin over l of
+// D + sum of incoming messages, interior nodes, lowest label on ties.
+template <typename T, typename M>
+__global__ void k_decode_fresh(const unsigned char *__restrict__ rec, int W, int H, int L, uint32_t rec_bytes,
+                               uint32_t d_bytes, uint32_t m_bytes, int32_t *labels) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t n = (size_t)(W - 2) * (H - 2);
+    if (idx >= n) return;
+    const int x = 1 + (int)(idx % (W - 2)), y = 1 + (int)(idx / (W - 2));
+    const unsigned char *r = rec + ((size_t)y * W + x) * rec_bytes;
+    const T *D = reinterpret_cast<const T *>(r);
+    bool z[4];
+    for (int d = 0; d < 4; ++d) z[d] = on_border(x + ddx(d), y + ddy(d), W, H);
+    T best = T(0);
+    int bl = 0;
+    for (int l = 0; l < L; ++l) {
+        T v = D[l];
+        for (int d = 0; d < 4; ++d) {
+            const M *m = reinterpret_cast<const M *>(r + d_bytes + d * m_bytes);
+            v = v + (z[d] ? T(0) : (T)msg_to_double(m[l]));
+        }
+        if (l == 0 || v < best) {
+            best = v;
+            bl = l;
+        }
+    }
+    labels[(size_t)y * W + x] = bl;
+}
+
+// Final level-0 messages into a dense [H][W][4][L] array of T (slot d = from
+// the neighbour in direction d; 0 where that neighbour is border or off-grid).
+template <typename T, typename M>
+__global__ void k_export(const unsigned char *__restrict__ rec, int W, int H, int L, uint32_t rec_bytes,
+                         uint32_t d_bytes, uint32_t m_bytes, T *__restrict__ dst) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t total = (size_t)W * H * 4 * L;
+    if (idx >= total) return;
+    const int l = (int)(idx % L);
+    const int d = (int)((idx / L) % 4);
+    const size_t node = idx / ((size_t)L * 4);
+    const int x = (int)(node % W), y = (int)(node / W);
+    const int qx = x + ddx(d), qy = y + ddy(d);
+    T v = T(0);
+    if (qx >= 0 && qy >= 0 && qx < W && qy < H && !on_border(qx, qy, W, H)) {
+        const M *m = reinterpret_cast<const M *>(rec + node * rec_bytes + d_bytes + d * m_bytes);
+        v = (T)msg_to_double(m[l]);
+    }
+    dst[idx] = v;
+}
+
+// One ICM node update, grid.cc:127-136 and icm.cc:10-34: one warp per node,
+// lane l handles labels l, l+32, ...; cost = D + V(l,f_S) + V(l,f_E) +
+// V(l,f_N) + V(l,f_W) in that order; argmin with the lowest label on ties.
+template <typename T>
+__device__ __forceinline__ int icm_node(const unsigned char *rec, int W, int H, int L, uint32_t rec_bytes,
+                                        const T *__restrict__ V, const int32_t *lab, int x, int y, int *status) {
+    const int lane = threadIdx.x & 31;
+    const T *D = reinterpret_cast<const T *>(rec + ((size_t)y * W + x) * rec_bytes);
+    int f[4];
+    for (int d = 0; d < 4; ++d) {
+        f[d] = lab[(size_t)(y + ddy(d)) * W + (x + ddx(d))];
+        if (f[d] < 0 || f[d] >= L) {
+            if (status && lane == 0) atomicOr(status, DEV_ERR_BOUNDS);
+            f[d] = 0;
+        }
+    }
+    T best = T(0);
+    int bl = 0x7fffffff;
+    for (int l = lane; l < L; l += 32) {
+        T c = D[l];
+        c += V[l + (size_t)L * f[0]];
+        c += V[l + (size_t)L * f[1]];
+        c += V[l + (size_t)L * f[2]];
+        c += V[l + (size_t)L * f[3]];
+        if (bl == 0x7fffffff || c < best) {
+            best = c;
+            bl = l;
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const T ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int ol = __shfl_xor_sync(0xffffffffu, bl, off);
+        if (ol != 0x7fffffff && (bl == 0x7fffffff || ob < best || (!(best < ob) && ol < bl))) {
+            best = ob;
+            bl = ol;
+        }
+    }
+    return bl;
+}
+
+template <typename T>
+__global__ void k_icm_sync(const unsigned char *__restrict__ rec, int W, int H, int L, uint32_t rec_bytes,
+                           const T *__restrict__ V, const int32_t *__restrict__ old_lab, int32_t *__restrict__ new_lab,
+                           int *status) {
+    const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const size_t n = (size_t)(W - 2) * (H - 2);
+    if (warp >= n) return;
+    const int x = 1 + (int)(warp % (W - 2)), y = 1 + (int)(warp / (W - 2));
+    const int bl = icm_node<T>(rec, W, H, L, rec_bytes, V, old_lab, x, y, status);
+    if ((threadIdx.x & 31) == 0) new_lab[(size_t)y * W + x] = bl;
+}
+
+// Raster Gauss-Seidel (icm.cc:40-67) as an exact wavefront: on anti-diagonal
+// s = x + y every node's west and north neighbours (diagonal s-1) are already
+// updated and its east and south neighbours (s+1) are not, exactly as in the
+// raster order, and nodes of one diagonal are never adjacent.
+template <typename T>
+__global__ void k_icm_diag(const unsigned char *__restrict__ rec, int W, int H, int L, uint32_t rec_bytes,
+                           const T *__restrict__ V, int32_t *lab, int s, int *status) {
+    const int warp = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int ylo = max(1, s - (W - 2)), yhi = min(H - 2, s - 1);
+    const int y = ylo + warp;
+    if (y > yhi) return;
+    const int x = s - y;
+    const int bl = icm_node<T>(rec, W, H, L, rec_bytes, V, lab, x, y, status);
+    if ((threadIdx.x & 31) == 0) lab[(size_t)y * W + x] = bl;
+}
+
+// Energy, grid.cc:102-125, in FP64: block partial sums over a fixed
+// grid-stride assignment, then one block adds the partials in a fixed tree,
+// so the result is identical from run to run.
+template <typename T>
+__global__ void k_energy_partial(const T *__restrict__ costs, size_t node_stride, size_t label_stride, int W, int H,
+                                 int L, const T *__restrict__ V, const int32_t *__restrict__ f, double *partials,
+                                 int *status) {
+    const size_t n = (size_t)(W - 2) * (H - 2);
+    double acc = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int x = 1 + (int)(i % (W - 2)), y = 1 + (int)(i / (W - 2));
+        const int fl = f[(size_t)y * W + x];
+        const int fn = f[(size_t)(y - 1) * W + x];
+        const int fe = f[(size_t)y * W + x + 1];
+        if (fl < 0 || fl >= L || fn < 0 || fn >= L || fe < 0 || fe >= L) {
+            atomicOr(status, DEV_ERR_BOUNDS);
+            continue;
+        }
+        acc += (double)costs[((size_t)y * W + x) * node_stride + (size_t)fl * label_stride];
+        acc += (double)V[fl + (size_t)L * fn];
+        acc += (double)V[fl + (size_t)L * fe];
+    }
+    __shared__ double red[kThreads / 32];
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < kThreads / 32 ? red[threadIdx.x] : 0.0;
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if (threadIdx.x == 0) partials[blockIdx.x] = v;
+    }
+}
+
+__global__ void k_energy_final(const double *partials, int n, double *out) {
+    __shared__ double red[kThreads];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += kThreads) acc += partials[i];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = kThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
+template <typename Ts, typename Td>
+__global__ void k_convert(const Ts *src, Td *dst, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (Td)src[i];
+}
+
+// D(x,y,d) = coef * min(|left(x,y) - right(max(x-d,0),y)|, cap), label-planar;
+// the operation sequence matches the numpy generator bit for bit.
+__global__ void k_stereo_costs(int W, int H, int L, const float *__restrict__ left, const float *__restrict__ right,
+                               float coef, float cap, float *__restrict__ costs) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t total = (size_t)W * H * L;
+    if (idx >= total) return;
+    const int x = (int)(idx % W);
+    const int y = (int)((idx / W) % H);
+    const int d = (int)(idx / ((size_t)W * H));
+    const float a = left[(size_t)y * W + x];
+    const float b = right[(size_t)y * W + max(x - d, 0)];
+    costs[idx] = coef * fminf(fabsf(a - b), cap);
+}
+
+}  // namespace
+
+RecordFormat make_format(int ctype, int store, int L) {
+    RecordFormat f;
+    f.ctype = ctype;
+    f.store = store;
+    f.L = L;
+    f.Lp = (L + 7) & ~7;
+    f.t_size = ctype == CT_F64 ? 8u : 4u;
+    f.m_size = store == ST_F16 ? 2u : f.t_size;
+    f.d_bytes = (uint32_t)f.Lp * f.t_size;
+    f.m_bytes = (uint32_t)f.Lp * f.m_size;
+    f.rec_bytes = f.d_bytes + 4 * f.m_bytes;
+    // Odd number of 16-byte chunks per shared-memory slot: eight consecutive
+    // slots then start in eight different bank groups.
+    f.slot_bytes = f.rec_bytes + (((f.rec_bytes / 16) % 2 == 0) ? 16u : 0u);
+    return f;
+}
+
+#define GINF_DISPATCH_T(f, ...)                                   \
+    switch ((f).ctype) {                                          \
+        case CT_F32: { using T = float; __VA_ARGS__ } break;      \
+        case CT_I32: { using T = int; __VA_ARGS__ } break;        \
+        case CT_F64: { using T = double; __VA_ARGS__ } break;     \
+        default: return cudaErrorInvalidValue;                    \
+    }
+
+#define GINF_DISPATCH_TM(f, ...)                                                        \
+    if ((f).store == ST_F16) {                                                          \
+        if ((f).ctype != CT_F32) return cudaErrorInvalidValue;                          \
+        using T = float; using M = __half; __VA_ARGS__                                  \
+    } else {                                                                            \
+        GINF_DISPATCH_T(f, using M = T; __VA_ARGS__)                                    \
+    }
+
+cudaError_t launch_costs_to_records(const RecordFormat &f, int cost_type, const void *src, int W, int H,
+                                    unsigned char *rec, cudaStream_t s) {
+    const dim3 grid((W + 31) / 32, H), block(32, 8);
+    GINF_DISPATCH_T(f, {
+        const size_t smem = (size_t)f.Lp * 33 * sizeof(T);
+        if (cost_type == CT_F32)
+            k_costs_to_records<float, T><<<grid, block, smem, s>>>(static_cast<const float *>(src), W, H, f.L, f.Lp,
+                                                                   rec, f.rec_bytes);
+        else
+            k_costs_to_records<int, T><<<grid, block, smem, s>>>(static_cast<const int *>(src), W, H, f.L, f.Lp, rec,
+                                                                 f.rec_bytes);
+    })
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pyramid(const RecordFormat &f, const unsigned char *frec, int fW, int fH, unsigned char *crec,
+                           int cW, int cH, cudaStream_t s) {
+    const size_t total = (size_t)cW * cH * f.Lp;
+    GINF_DISPATCH_T(f, { k_pyramid<T><<<blocks_for(total), kThreads, 0, s>>>(frec, fW, fH, crec, cW, cH, f.L, f.Lp,
+                                                                            f.rec_bytes); })
+    return cudaGetLastError();
+}
+
+cudaError_t launch_init_messages(const RecordFormat &f, unsigned char *rec, int W, int H, const unsigned char *crec,
+                                 int cW, int cH, cudaStream_t s) {
+    const size_t total = (size_t)W * H * 4 * (f.m_bytes / 16);
+    k_init_messages<<<blocks_for(total), kThreads, 0, s>>>(rec, W, H, crec, cW, cH, f.rec_bytes, f.d_bytes,
+                                                           f.m_bytes);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_interior(int32_t *labels, int W, int H, int32_t value, cudaStream_t s) {
+    if (W < 3 || H < 3) return cudaSuccess;
+    const size_t n = (size_t)(W - 2) * (H - 2);
+    k_fill_interior<<<blocks_for(n), kThreads, 0, s>>>(labels, W, H, value);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_decode_fresh(const RecordFormat &f, const unsigned char *rec, int W, int H, int32_t *labels,
+                                cudaStream_t s) {
+    if (W < 3 || H < 3) return cudaSuccess;
+    const size_t n = (size_t)(W - 2) * (H - 2);
+    GINF_DISPATCH_TM(f, { k_decode_fresh<T, M><<<blocks_for(n), kThreads, 0, s>>>(rec, W, H, f.L, f.rec_bytes,
+                                                                                  f.d_bytes, f.m_bytes, labels); })
+    return cudaGetLastError();
+}
+
+cudaError_t launch_export_messages(const RecordFormat &f, const unsigned char *rec, int W, int H, void *dst,
+                                   cudaStream_t s) {
+    const size_t total = (size_t)W * H * 4 * f.L;
+    GINF_DISPATCH_TM(f, { k_export<T, M><<<blocks_for(total), kThreads, 0, s>>>(rec, W, H, f.L, f.rec_bytes,
+                                                                                f.d_bytes, f.m_bytes,
+                                                                                static_cast<T *>(dst)); })
+    return cudaGetLastError();
+}
+
+cudaError_t launch_icm_sync(const RecordFormat &f, const unsigned char *rec, int W, int H, const void *V,
+                            const int32_t *old_labels, int32_t *new_labels, int *status, cudaStream_t s) {
+    if (W < 3 || H < 3) return cudaSuccess;
+    const size_t n = (size_t)(W - 2) * (H - 2);
+    GINF_DISPATCH_T(f, { k_icm_sync<T><<<blocks_for(n * 32), kThreads, 0, s>>>(
+                             rec, W, H, f.L, f.rec_bytes, static_cast<const T *>(V), old_labels, new_labels, status); })
+    return cudaGetLastError();
+}
+
+cudaError_t launch_icm_async_diag(const RecordFormat &f, const unsigned char *rec, int W, int H, const void *V,
+                                  int32_t *labels, int diag, int *status, cudaStream_t s) {
+    const int ylo = diag - (W - 2) > 1 ? diag - (W - 2) : 1;
+    const int yhi = diag - 1 < H - 2 ? diag - 1 : H - 2;
+    if (yhi < ylo) return cudaSuccess;
+    const size_t n = (size_t)(yhi - ylo + 1);
+    GINF_DISPATCH_T(f, { k_icm_diag<T><<<blocks_for(n * 32), kThreads, 0, s>>>(rec, W, H, f.L, f.rec_bytes,
+                                                                             static_cast<const T *>(V), labels, diag,
+                                                                             status); })
+    return cudaGetLastError();
+}
+
+int energy_num_partials(int W, int H) {
+    const size_t n = (W > 2 && H > 2) ? (size_t)(W - 2) * (H - 2) : 0;
+    size_t b = (n + kThreads - 1) / kThreads;
+    if (b > 2048) b = 2048;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+cudaError_t launch_energy(int ctype, const void *costs, size_t node_stride, size_t label_stride, int W, int H, int L,
+                          const void *V, const int32_t *labels, double *partials, int num_partials, double *out,
+                          int *status, cudaStream_t s) {
+    if (W < 3 || H < 3) {
+        return cudaMemsetAsync(out, 0, sizeof(double), s);
+    }
+    RecordFormat f;
+    f.ctype = ctype;
+    GINF_DISPATCH_T(f, { k_energy_partial<T><<<num_partials, kThreads, 0, s>>>(
+                             static_cast<const T *>(costs), node_stride, label_stride, W, H, L,
+                             static_cast<const T *>(V), labels, partials, status); })
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_energy_final<<<1, kThreads, 0, s>>>(partials, num_partials, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_convert_table(int src_type, int dst_type, const void *src, void *dst, int n, cudaStream_t s) {
+    const unsigned b = blocks_for((size_t)n);
+    if (src_type == CT_F32 && dst_type == CT_F64)
+        k_convert<float, double><<<b, kThreads, 0, s>>>(static_cast<const float *>(src), static_cast<double *>(dst), n);
+    else if (src_type == CT_I32 && dst_type == CT_F64)
+        k_convert<int, double><<<b, kThreads, 0, s>>>(static_cast<const int *>(src), static_cast<double *>(dst), n);
+    else if (src_type == CT_I32 && dst_type == CT_F32)
+        k_convert<int, float><<<b, kThreads, 0, s>>>(static_cast<const int *>(src), static_cast<float *>(dst), n);
+    else if (src_type == CT_F32 && dst_type == CT_I32)
+        k_convert<float, int><<<b, kThreads, 0, s>>>(static_cast<const float *>(src), static_cast<int *>(dst), n);
+    else
+        return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stereo_costs(int W, int H, int L, const float *left, const float *right, float coef, float cap,
+                                float *costs, cudaStream_t s) {
+    const size_t total = (size_t)W * H * L;
+    k_stereo_costs<<<blocks_for(total), kThreads, 0, s>>>(W, H, L, left, right, coef, cap, costs);
+    return cudaGetLastError();
+}
+
+}  // namespace ginf_gpu

@@ -1,0 +1,764 @@
+// capi.cu -- implementation of the C ABI declared in include/ginf_gb300.h.
+//
+// Host-side driver of the inference path: argument checks, the workspace
+// arena, host<->device copies, the HBP level loop (bp.cc:86-180 /
+// bp.cu:133-223), ICM (icm.cc:4-67), the energy (grid.cc:102-125) and status
+// reporting.  Every entry point is synchronous, like the reference (its
+// cudaMemcpy calls block, gpu.h:59,123): it returns after its stream has
+// drained, with the device status word checked.
+#include <cuda_fp16.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "ginf_gb300.h"
+#include "ginf_internal.h"
+
+using namespace ginf_gpu;
+
+namespace ginf_gpu {
+template <typename T, typename M>
+cudaError_t launch_sweep_tm(const RecordFormat &, const SweepConfig &, const SweepParams &, cudaStream_t, int);
+
+cudaError_t launch_sweep(const RecordFormat &f, const SweepConfig &cfg, SweepParams p, cudaStream_t s, int num_sms) {
+    if (f.store == ST_F16) return launch_sweep_tm<float, __half>(f, cfg, p, s, num_sms);
+    switch (f.ctype) {
+        case CT_F32: return launch_sweep_tm<float, float>(f, cfg, p, s, num_sms);
+        case CT_I32: return launch_sweep_tm<int, int>(f, cfg, p, s, num_sms);
+        case CT_F64: return launch_sweep_tm<double, double>(f, cfg, p, s, num_sms);
+    }
+    return cudaErrorInvalidValue;
+}
+
+bool sweep_supported(const RecordFormat &f) { return f.L >= 2 && f.L <= kMaxLabels; }
+}  // namespace ginf_gpu
+
+namespace {
+
+thread_local std::string g_last_error;
+
+ginf_status fail(ginf_status s, const std::string &msg) {
+    g_last_error = msg;
+    return s;
+}
+
+ginf_status cuda_fail(cudaError_t e, const char *what) {
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return fail(GINF_ERR_OUT_OF_MEMORY, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+    return fail(GINF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define GINF_CK(call)                                          \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);    \
+    } while (0)
+
+#define GINF_TRY(call)                                         \
+    do {                                                       \
+        ginf_status s_ = (call);                               \
+        if (s_ != GINF_OK) return s_;                          \
+    } while (0)
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+// Reusable device state of one caller (thread / stream).
+struct ginf_workspace {
+    int device = -1;
+    int num_sms = 0;
+    unsigned char *arena = nullptr;
+    size_t arena_bytes = 0;
+    int *status_host = nullptr;   // pinned
+    double *energy_host = nullptr;  // pinned
+    cudaEvent_t ev[10] = {};
+    bool events = false;
+};
+
+namespace {
+
+enum { EV_START, EV_UPLOAD, EV_PREPARE, EV_L0_START, EV_SWEEPS, EV_ICM, EV_ENERGY, EV_END, EV_COUNT };
+
+ginf_status check_device(ginf_workspace *ws) {
+    int dev = 0;
+    GINF_CK(cudaGetDevice(&dev));
+    if (ws->device == dev) return GINF_OK;
+    cudaDeviceProp prop;
+    cudaError_t e = cudaGetDeviceProperties(&prop, dev);
+    if (e != cudaSuccess) return fail(GINF_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    if (prop.major * 10 + prop.minor != 103)
+        return fail(GINF_ERR_NO_DEVICE, std::string("this library is built for sm_103 (GB300); device is ") +
+                                            prop.name);
+    ws->device = dev;
+    ws->num_sms = prop.multiProcessorCount;
+    return GINF_OK;
+}
+
+ginf_status ws_init(ginf_workspace *ws) {
+    GINF_TRY(check_device(ws));
+    if (!ws->status_host) {
+        GINF_CK(cudaMallocHost(&ws->status_host, 64));
+        ws->energy_host = reinterpret_cast<double *>(ws->status_host + 8);
+    }
+    if (!ws->events) {
+        for (int i = 0; i < EV_COUNT; ++i) GINF_CK(cudaEventCreate(&ws->ev[i]));
+        ws->events = true;
+    }
+    return GINF_OK;
+}
+
+// Carves sub-buffers out of one growing device allocation.
+struct Arena {
+    std::vector<size_t> sizes;
+    size_t add(size_t bytes) {
+        sizes.push_back(align_up(bytes, 256));
+        return sizes.size() - 1;
+    }
+    size_t total() const {
+        size_t t = 0;
+        for (size_t s : sizes) t += s;
+        return t;
+    }
+    unsigned char *ptr(unsigned char *base, size_t id) const {
+        size_t off = 0;
+        for (size_t i = 0; i < id; ++i) off += sizes[i];
+        return base + off;
+    }
+};
+
+ginf_status ws_reserve(ginf_workspace *ws, size_t bytes) {
+    if (bytes <= ws->arena_bytes) return GINF_OK;
+    if (ws->arena) {
+        cudaFree(ws->arena);
+        ws->arena = nullptr;
+        ws->arena_bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&ws->arena, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GINF_ERR_OUT_OF_MEMORY, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " +
+                                                cudaGetErrorString(e));
+    }
+    ws->arena_bytes = bytes;
+    return GINF_OK;
+}
+
+// Per-call workspace: the caller's, or a temporary one freed on exit.
+struct WsGuard {
+    ginf_workspace *ws;
+    bool owned;
+    explicit WsGuard(ginf_workspace *w) : ws(w), owned(w == nullptr) {
+        if (owned) ws = new ginf_workspace();
+    }
+    ~WsGuard() {
+        if (owned) ginf_workspace_destroy(ws);
+    }
+};
+
+size_t type_size(int t) { return t == GINF_F64 ? 8 : 4; }
+
+ginf_status check_grid(const ginf_grid *g) {
+    if (!g) return fail(GINF_ERR_INVALID_ARGUMENT, "grid is NULL");
+    if (g->width < 1 || g->height < 1) return fail(GINF_ERR_INVALID_ARGUMENT, "grid width/height must be >= 1");
+    if (g->num_labels < 2)
+        return fail(GINF_ERR_INVALID_ARGUMENT,
+                    "num_labels must be >= 2 (the reference reads V(0,1) out of bounds for one label, bp.cc:35)");
+    if (g->cost_type != GINF_F32 && g->cost_type != GINF_I32)
+        return fail(GINF_ERR_INVALID_ARGUMENT, "cost_type must be GINF_F32 or GINF_I32");
+    if (g->sm_model < GINF_SM_EXPLICIT || g->sm_model > GINF_SM_TRUNC_QUAD)
+        return fail(GINF_ERR_INVALID_ARGUMENT, "unknown smoothness model");
+    if (g->memory != GINF_HOST && g->memory != GINF_DEVICE)
+        return fail(GINF_ERR_INVALID_ARGUMENT, "memory must be GINF_HOST or GINF_DEVICE");
+    if (!g->data_costs || !g->sm_costs) return fail(GINF_ERR_INVALID_ARGUMENT, "data_costs / sm_costs is NULL");
+    const double elems = (double)g->width * g->height * g->num_labels;
+    if (elems > 4.0e10) return fail(GINF_ERR_INVALID_ARGUMENT, "grid too large");
+    return GINF_OK;
+}
+
+struct Resolved {
+    int ctype;      // compute type
+    int store;      // ST_*
+    int mode;       // Mode
+    int norm_min;
+    int decode;
+    SweepConfig cfg;
+    cudaStream_t stream;
+};
+
+ginf_status resolve(const ginf_grid *g, const ginf_options *o, Resolved &r) {
+    ginf_options d;
+    ginf_default_options(&d);
+    if (!o) o = &d;
+    r.ctype = o->compute_type < 0 ? g->cost_type : o->compute_type;
+    if (r.ctype != GINF_F32 && r.ctype != GINF_I32 && r.ctype != GINF_F64)
+        return fail(GINF_ERR_INVALID_ARGUMENT, "unknown compute_type");
+    if (o->msg_store != GINF_STORE_NATIVE && o->msg_store != GINF_STORE_F16)
+        return fail(GINF_ERR_INVALID_ARGUMENT, "unknown msg_store");
+    if (o->msg_store == GINF_STORE_F16 && r.ctype != GINF_F32)
+        return fail(GINF_ERR_UNSUPPORTED, "the FP16 message store needs FP32 arithmetic");
+    r.store = o->msg_store == GINF_STORE_F16 ? ST_F16 : ST_NATIVE;
+    if (o->msg_rule != GINF_RULE_REFERENCE && o->msg_rule != GINF_RULE_STANDARD)
+        return fail(GINF_ERR_INVALID_ARGUMENT, "unknown msg_rule");
+    if (o->decode != GINF_DECODE_STALE && o->decode != GINF_DECODE_FRESH)
+        return fail(GINF_ERR_INVALID_ARGUMENT, "unknown decode");
+    if (o->normalize != GINF_NORM_MEAN && o->normalize != GINF_NORM_MIN)
+        return fail(GINF_ERR_INVALID_ARGUMENT, "unknown normalize");
+    const int m = g->sm_model;
+    if (m == GINF_SM_POTTS || m == GINF_SM_TRUNC_LINEAR) r.mode = MODE_LINEAR;
+    else if (o->msg_rule == GINF_RULE_REFERENCE) r.mode = MODE_REF_MINCONV;
+    else if (m == GINF_SM_TRUNC_QUAD && r.ctype != GINF_I32) r.mode = MODE_STD_QUAD;
+    else r.mode = MODE_STD_MINCONV;
+    r.norm_min = (o->normalize == GINF_NORM_MIN || r.store == ST_F16) ? 1 : 0;
+    r.decode = o->decode;
+    r.cfg.nt = o->tile_nodes == 64 ? 64 : 32;
+    r.cfg.stages = o->stages == 2 ? 2 : 1;
+    if (o->tile_nodes != 0 && o->tile_nodes != 32 && o->tile_nodes != 64)
+        return fail(GINF_ERR_INVALID_ARGUMENT, "tile_nodes must be 0, 32 or 64");
+    if (o->stages < 0 || o->stages > 2) return fail(GINF_ERR_INVALID_ARGUMENT, "stages must be 0, 1 or 2");
+    r.stream = static_cast<cudaStream_t>(o->stream);
+    return GINF_OK;
+}
+
+struct Level {
+    int W, H;
+    size_t off;  // byte offset within the records buffer
+};
+
+std::vector<Level> level_sizes(int W, int H, int levels, size_t rec_bytes, size_t &total) {
+    std::vector<Level> lv(levels);
+    size_t off = 0;
+    for (int t = 0; t < levels; ++t) {
+        lv[t].W = t == 0 ? W : (lv[t - 1].W + 1) / 2;  // ceil(w/2), bp.cc:101-102
+        lv[t].H = t == 0 ? H : (lv[t - 1].H + 1) / 2;
+        lv[t].off = off;
+        off += align_up((size_t)lv[t].W * lv[t].H * rec_bytes, 256);
+    }
+    total = off;
+    return lv;
+}
+
+// Everything a BP / ICM / energy pipeline run needs on the device.
+struct Prepared {
+    RecordFormat f;
+    std::vector<Level> lv;
+    unsigned char *rec = nullptr;  // records of all levels
+    void *Vt = nullptr;            // table in the compute type
+    int32_t *lab = nullptr;        // device labels (caller's or a copy)
+    int32_t *lab2 = nullptr;       // second label buffer (ICM ping-pong)
+    double *partials = nullptr;    // energy partials, status word follows
+    int num_partials = 0;
+    int *status = nullptr;
+    double *energy = nullptr;
+    void *msgs_stage = nullptr;
+    int64_t launches = 0;
+};
+
+struct Call {
+    ginf_workspace *ws;
+    const ginf_grid *g;
+    Resolved r;
+    ginf_stats *stats;
+    int64_t launches = 0;
+    int64_t h2d = 0, d2h = 0;
+    void ev(int i) {
+        if (stats) cudaEventRecord(ws->ev[i], r.stream);
+    }
+};
+
+// Uploads costs and table, builds level-0 records and the pyramid.
+// levels == 0 builds a D-only record (ICM / energy).
+ginf_status prepare(Call &c, Prepared &P, int levels, bool want_lab2, const int32_t *labels_in, int32_t *labels_dev) {
+    const ginf_grid *g = c.g;
+    const int W = g->width, H = g->height, L = g->num_labels;
+    const bool bp = levels > 0;
+    P.f = make_format(c.r.ctype, c.r.store, L);
+    if (!bp) {
+        P.f.m_bytes = 0;
+        P.f.rec_bytes = P.f.d_bytes;
+    }
+    size_t rec_total = 0;
+    P.lv = level_sizes(W, H, bp ? levels : 1, P.f.rec_bytes, rec_total);
+    const size_t cost_bytes = (size_t)W * H * L * type_size(g->cost_type);
+    const size_t table_in = (size_t)L * L * type_size(g->cost_type);
+    const size_t table_t = (size_t)L * L * P.f.t_size;
+    const size_t lab_bytes = (size_t)W * H * sizeof(int32_t);
+    P.num_partials = energy_num_partials(W, H);
+
+    Arena a;
+    const size_t id_rec = a.add(rec_total);
+    const size_t id_stage = g->memory == GINF_HOST ? a.add(cost_bytes) : 0;
+    const size_t id_tin = a.add(table_in);
+    const size_t id_t = a.add(table_t);
+    const size_t id_lab = (labels_dev == nullptr) ? a.add(lab_bytes) : 0;
+    const size_t id_lab2 = want_lab2 ? a.add(lab_bytes) : 0;
+    const size_t id_part = a.add(sizeof(double) * (P.num_partials + 1) + 64);
+    const bool host = g->memory == GINF_HOST;
+    GINF_TRY(ws_reserve(c.ws, a.total()));
+    unsigned char *base = c.ws->arena;
+    P.rec = a.ptr(base, id_rec);
+    P.Vt = a.ptr(base, id_t);
+    P.lab = labels_dev ? labels_dev : reinterpret_cast<int32_t *>(a.ptr(base, id_lab));
+    P.lab2 = want_lab2 ? reinterpret_cast<int32_t *>(a.ptr(base, id_lab2)) : nullptr;
+    P.partials = reinterpret_cast<double *>(a.ptr(base, id_part));
+    P.status = reinterpret_cast<int *>(P.partials + P.num_partials);
+    P.energy = P.partials + P.num_partials + 1;
+    cudaStream_t s = c.r.stream;
+
+    GINF_CK(cudaMemsetAsync(P.status, 0, sizeof(int), s));
+    // Costs and table on the device, in the caller's element type.
+    const void *costs_dev = g->data_costs;
+    const void *table_dev = g->sm_costs;
+    if (host) {
+        unsigned char *stage = a.ptr(base, id_stage);
+        GINF_CK(cudaMemcpyAsync(stage, g->data_costs, cost_bytes, cudaMemcpyHostToDevice, s));
+        unsigned char *tin = a.ptr(base, id_tin);
+        GINF_CK(cudaMemcpyAsync(tin, g->sm_costs, table_in, cudaMemcpyHostToDevice, s));
+        c.h2d += cost_bytes + table_in;
+        costs_dev = stage;
+        table_dev = tin;
+    }
+    if (labels_in) {
+        // Labels the device copy starts from (border values are read by ICM
+        // and preserved for the caller).
+        GINF_CK(cudaMemcpyAsync(P.lab, labels_in, lab_bytes, host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                                s));
+        if (host) c.h2d += lab_bytes;
+    }
+    c.ev(EV_UPLOAD);
+    if (c.r.ctype == g->cost_type) {
+        GINF_CK(cudaMemcpyAsync(P.Vt, table_dev, table_t, cudaMemcpyDeviceToDevice, s));
+    } else {
+        GINF_CK(launch_convert_table(g->cost_type, c.r.ctype, table_dev, P.Vt, L * L, s));
+        ++c.launches;
+    }
+    GINF_CK(launch_costs_to_records(P.f, g->cost_type, costs_dev, W, H, P.rec, s));
+    ++c.launches;
+    for (int t = 1; t < (int)P.lv.size(); ++t) {
+        GINF_CK(launch_pyramid(P.f, P.rec + P.lv[t - 1].off, P.lv[t - 1].W, P.lv[t - 1].H, P.rec + P.lv[t].off,
+                               P.lv[t].W, P.lv[t].H, s));
+        ++c.launches;
+    }
+    c.ev(EV_PREPARE);
+    return GINF_OK;
+}
+
+// The HBP level loop on prepared records: bp.cc:121-166 (bp.cu:180-205).
+ginf_status run_bp(Call &c, Prepared &P, int iters, int64_t &nli) {
+    const RecordFormat &f = P.f;
+    cudaStream_t s = c.r.stream;
+    const int T = (int)P.lv.size();
+    const bool stale = c.r.decode == GINF_DECODE_STALE;
+    const int W0 = P.lv[0].W, H0 = P.lv[0].H;
+    // Nodes a level-0 colour never updates keep the argmin of a zero belief.
+    if (stale && iters < 2 && W0 >= 3 && H0 >= 3) {
+        GINF_CK(launch_fill_interior(P.lab, W0, H0, 0, s));
+        ++c.launches;
+    }
+    nli = 0;
+    for (int t = T - 1; t >= 0; --t) {
+        const Level &lv = P.lv[t];
+        unsigned char *rec = P.rec + lv.off;
+        const bool interior = lv.W >= 3 && lv.H >= 3;
+        // Two or more half-sweeps write every slot an interior sender owns, so
+        // the first sweep can read its inputs straight from the coarser level
+        // (or as zeros at the top) and no initialisation pass is needed.
+        const bool fused = iters >= 2 && interior;
+        int first = RD_OWN;
+        if (t == T - 1) {
+            if (fused) first = RD_ZERO;
+            else {
+                GINF_CK(launch_init_messages(f, rec, lv.W, lv.H, nullptr, 0, 0, s));
+                ++c.launches;
+            }
+        } else {
+            const Level &cl = P.lv[t + 1];
+            if (fused) first = RD_COARSE;
+            else {
+                GINF_CK(launch_init_messages(f, rec, lv.W, lv.H, P.rec + cl.off, cl.W, cl.H, s));
+                ++c.launches;
+            }
+        }
+        if (t == 0) c.ev(EV_L0_START);
+        if (!interior) continue;
+        const int n1 = (lv.W - 3) / 2 + 1;
+        SweepParams p{};
+        p.W = lv.W;
+        p.H = lv.H;
+        p.L = f.L;
+        p.Lp = f.Lp;
+        p.rec_bytes = f.rec_bytes;
+        p.d_bytes = f.d_bytes;
+        p.m_bytes = f.m_bytes;
+        p.slot_bytes = f.slot_bytes;
+        p.rec = rec;
+        if (t + 1 < T) {
+            p.crec = P.rec + P.lv[t + 1].off;
+            p.cW = P.lv[t + 1].W;
+            p.cH = P.lv[t + 1].H;
+        }
+        p.mode = c.r.mode;
+        p.norm_min = c.r.norm_min;
+        p.V = P.Vt;
+        p.labels = P.lab;
+        p.tiles_per_row = (n1 + c.r.cfg.nt - 1) / c.r.cfg.nt;
+        p.num_tiles = (lv.H - 2) * p.tiles_per_row;
+        p.status = P.status;
+        for (int it = 0; it < iters; ++it) {
+            p.iter = it;
+            p.read_mode = it == 0 ? first : RD_OWN;
+            p.write_labels = (t == 0 && stale && it >= iters - 2) ? 1 : 0;
+            GINF_CK(launch_sweep(f, c.r.cfg, p, s, c.ws->num_sms));
+            ++c.launches;
+            if (t == 0 && c.stats) ++c.stats->level0_sweep_launches;
+        }
+        nli += (int64_t)lv.W * lv.H * f.L * iters;
+    }
+    if (!stale && W0 >= 3 && H0 >= 3) {
+        GINF_CK(launch_decode_fresh(f, P.rec, W0, H0, P.lab, s));
+        ++c.launches;
+    }
+    c.ev(EV_SWEEPS);
+    return GINF_OK;
+}
+
+// Jacobi ICM (icm.cc:4-38) from P.lab, result in P.lab.
+ginf_status run_icm_sync(Call &c, Prepared &P, int iters) {
+    const int W = c.g->width, H = c.g->height;
+    const size_t lab_bytes = (size_t)W * H * sizeof(int32_t);
+    cudaStream_t s = c.r.stream;
+    if (iters <= 0 || W < 3 || H < 3) return GINF_OK;
+    GINF_CK(cudaMemcpyAsync(P.lab2, P.lab, lab_bytes, cudaMemcpyDeviceToDevice, s));
+    int32_t *src = P.lab, *dst = P.lab2;
+    for (int it = 0; it < iters; ++it) {
+        GINF_CK(launch_icm_sync(P.f, P.rec, W, H, P.Vt, src, dst, P.status, s));
+        ++c.launches;
+        std::swap(src, dst);
+    }
+    if (src != P.lab) GINF_CK(cudaMemcpyAsync(P.lab, src, lab_bytes, cudaMemcpyDeviceToDevice, s));
+    return GINF_OK;
+}
+
+ginf_status run_icm_async(Call &c, Prepared &P, int iters) {
+    const int W = c.g->width, H = c.g->height;
+    if (iters <= 0 || W < 3 || H < 3) return GINF_OK;
+    for (int it = 0; it < iters; ++it)
+        for (int diag = 2; diag <= (W - 2) + (H - 2); ++diag) {
+            GINF_CK(launch_icm_async_diag(P.f, P.rec, W, H, P.Vt, P.lab, diag, P.status, c.r.stream));
+            ++c.launches;
+        }
+    return GINF_OK;
+}
+
+ginf_status run_energy(Call &c, Prepared &P) {
+    const int W = c.g->width, H = c.g->height;
+    GINF_CK(launch_energy(P.f.ctype, P.rec, P.f.rec_bytes / P.f.t_size, 1, W, H, P.f.L, P.Vt, P.lab, P.partials,
+                          P.num_partials, P.energy, P.status, c.r.stream));
+    c.launches += 2;
+    return GINF_OK;
+}
+
+// Drains the stream, reads the device status word, fills the stats.
+ginf_status finish(Call &c, int64_t nli) {
+    cudaStream_t s = c.r.stream;
+    GINF_CK(cudaStreamSynchronize(s));
+    if (c.stats) {
+        ginf_stats *st = c.stats;
+        auto ms = [&](int a, int b) {
+            float v = 0.f;
+            if (cudaEventElapsedTime(&v, c.ws->ev[a], c.ws->ev[b]) != cudaSuccess) {
+                cudaGetLastError();
+                return 0.0;
+            }
+            return (double)v;
+        };
+        st->total_ms = ms(EV_START, EV_END);
+        st->upload_ms = ms(EV_START, EV_UPLOAD);
+        st->prepare_ms = ms(EV_UPLOAD, EV_PREPARE);
+        st->sweep_ms = ms(EV_PREPARE, EV_SWEEPS);
+        st->level0_sweep_ms = ms(EV_L0_START, EV_SWEEPS);
+        st->icm_ms = ms(EV_SWEEPS, EV_ICM);
+        st->energy_ms = ms(EV_ICM, EV_ENERGY);
+        st->download_ms = ms(EV_ENERGY, EV_END);
+        st->kernel_launches = c.launches;
+        st->node_label_iters = nli;
+        st->h2d_bytes = c.h2d;
+        st->d2h_bytes = c.d2h;
+    }
+    return GINF_OK;
+}
+
+ginf_status read_status(Call &c, Prepared &P) {
+    GINF_CK(cudaMemcpyAsync(c.ws->status_host, P.status, sizeof(int), cudaMemcpyDeviceToHost, c.r.stream));
+    GINF_CK(cudaStreamSynchronize(c.r.stream));
+    const int st = *c.ws->status_host;
+    if (st & DEV_ERR_TIMEOUT) return fail(GINF_ERR_TIMEOUT, "a device-side wait exceeded its time limit");
+    if (st & DEV_ERR_BOUNDS) return fail(GINF_ERR_INVALID_ARGUMENT, "a label is outside [0, num_labels)");
+    return GINF_OK;
+}
+
+void begin(Call &c) {
+    if (c.stats) {
+        std::memset(c.stats, 0, sizeof(ginf_stats));
+        c.ev(EV_START);
+    }
+}
+
+ginf_status labels_to_caller(Call &c, Prepared &P, int32_t *labels, bool interior_only) {
+    const ginf_grid *g = c.g;
+    if (g->memory != GINF_HOST) return GINF_OK;  // written in place
+    const int W = g->width, H = g->height;
+    cudaStream_t s = c.r.stream;
+    if (interior_only) {
+        if (W < 3 || H < 3) return GINF_OK;
+        GINF_CK(cudaMemcpy2DAsync(labels + W + 1, W * sizeof(int32_t), P.lab + W + 1, W * sizeof(int32_t),
+                                  (W - 2) * sizeof(int32_t), H - 2, cudaMemcpyDeviceToHost, s));
+        c.d2h += (int64_t)(W - 2) * (H - 2) * 4;
+    } else {
+        GINF_CK(cudaMemcpyAsync(labels, P.lab, (size_t)W * H * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        c.d2h += (int64_t)W * H * 4;
+    }
+    return GINF_OK;
+}
+
+ginf_status export_msgs(Call &c, Prepared &P, const ginf_options *o) {
+    if (!o || !o->msgs_out) return GINF_OK;
+    const ginf_grid *g = c.g;
+    const int W = g->width, H = g->height, L = g->num_labels;
+    const size_t bytes = (size_t)W * H * 4 * L * P.f.t_size;
+    cudaStream_t s = c.r.stream;
+    if (g->memory == GINF_DEVICE) {
+        GINF_CK(launch_export_messages(P.f, P.rec, W, H, o->msgs_out, s));
+        ++c.launches;
+        return GINF_OK;
+    }
+    void *tmp = nullptr;
+    GINF_CK(cudaMallocAsync(&tmp, bytes, s));
+    cudaError_t e = launch_export_messages(P.f, P.rec, W, H, tmp, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(o->msgs_out, tmp, bytes, cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(tmp, s);
+    if (e != cudaSuccess) return cuda_fail(e, "message export");
+    ++c.launches;
+    c.d2h += bytes;
+    return GINF_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+
+extern "C" {
+
+const char *ginf_version(void) { return "gridinfcuda-gb300 0.1 (sm_103a)"; }
+
+const char *ginf_last_error(void) { return g_last_error.c_str(); }
+
+void ginf_default_options(ginf_options *opt) {
+    if (!opt) return;
+    std::memset(opt, 0, sizeof(*opt));
+    opt->msg_rule = GINF_RULE_REFERENCE;
+    opt->msg_store = GINF_STORE_NATIVE;
+    opt->decode = GINF_DECODE_STALE;
+    opt->normalize = GINF_NORM_MEAN;
+    opt->compute_type = -1;
+}
+
+ginf_status ginf_workspace_create(ginf_workspace **ws) {
+    if (!ws) return fail(GINF_ERR_INVALID_ARGUMENT, "ws is NULL");
+    *ws = new ginf_workspace();
+    return GINF_OK;
+}
+
+ginf_status ginf_workspace_destroy(ginf_workspace *ws) {
+    if (!ws) return GINF_OK;
+    if (ws->arena) cudaFree(ws->arena);
+    if (ws->status_host) cudaFreeHost(ws->status_host);
+    if (ws->events)
+        for (int i = 0; i < EV_COUNT; ++i) cudaEventDestroy(ws->ev[i]);
+    delete ws;
+    return GINF_OK;
+}
+
+ginf_status ginf_decode_hbp(ginf_workspace *wsp, const ginf_grid *grid, int32_t num_levels, int32_t iters_per_level,
+                            int32_t *labels, const ginf_options *opt, ginf_stats *stats) {
+    g_last_error.clear();
+    GINF_TRY(check_grid(grid));
+    if (num_levels < 1) return fail(GINF_ERR_INVALID_ARGUMENT, "num_levels must be >= 1");
+    if (iters_per_level < 0) return fail(GINF_ERR_INVALID_ARGUMENT, "iters_per_level must be >= 0");
+    if (!labels) return fail(GINF_ERR_INVALID_ARGUMENT, "labels is NULL");
+    Call c;
+    GINF_TRY(resolve(grid, opt, c.r));
+    if (grid->num_labels > kMaxLabels)
+        return fail(GINF_ERR_UNSUPPORTED, "num_labels above " + std::to_string(kMaxLabels) + " is not compiled in");
+    WsGuard guard(wsp);
+    c.ws = guard.ws;
+    c.g = grid;
+    c.stats = stats;
+    GINF_TRY(ws_init(c.ws));
+    begin(c);
+    Prepared P;
+    const bool host = grid->memory == GINF_HOST;
+    // Device labels: the caller's buffer, or a copy holding the caller's labels
+    // so the untouched border goes back unchanged.
+    GINF_TRY(prepare(c, P, num_levels, false, nullptr, host ? nullptr : labels));
+    int64_t nli = 0;
+    GINF_TRY(run_bp(c, P, iters_per_level, nli));
+    c.ev(EV_ICM);
+    c.ev(EV_ENERGY);
+    GINF_TRY(export_msgs(c, P, opt));
+    GINF_TRY(labels_to_caller(c, P, labels, true));
+    c.ev(EV_END);
+    GINF_TRY(read_status(c, P));
+    return finish(c, nli);
+}
+
+ginf_status ginf_decode_icm(ginf_workspace *wsp, const ginf_grid *grid, const int32_t *initial, int32_t iters,
+                            int32_t asynchronous, int32_t *result, const ginf_options *opt, ginf_stats *stats) {
+    g_last_error.clear();
+    GINF_TRY(check_grid(grid));
+    if (!initial || !result) return fail(GINF_ERR_INVALID_ARGUMENT, "initial / result is NULL");
+    if (iters < 0) return fail(GINF_ERR_INVALID_ARGUMENT, "iters must be >= 0");
+    Call c;
+    GINF_TRY(resolve(grid, opt, c.r));
+    WsGuard guard(wsp);
+    c.ws = guard.ws;
+    c.g = grid;
+    c.stats = stats;
+    GINF_TRY(ws_init(c.ws));
+    begin(c);
+    Prepared P;
+    const bool host = grid->memory == GINF_HOST;
+    GINF_TRY(prepare(c, P, 0, !asynchronous, initial, host ? nullptr : result));
+    c.ev(EV_L0_START);
+    c.ev(EV_SWEEPS);
+    if (asynchronous) GINF_TRY(run_icm_async(c, P, iters));
+    else GINF_TRY(run_icm_sync(c, P, iters));
+    c.ev(EV_ICM);
+    c.ev(EV_ENERGY);
+    GINF_TRY(labels_to_caller(c, P, result, false));
+    c.ev(EV_END);
+    GINF_TRY(read_status(c, P));
+    return finish(c, 0);
+}
+
+ginf_status ginf_energy(ginf_workspace *wsp, const ginf_grid *grid, const int32_t *labels, double *energy,
+                        const ginf_options *opt) {
+    g_last_error.clear();
+    GINF_TRY(check_grid(grid));
+    if (!labels || !energy) return fail(GINF_ERR_INVALID_ARGUMENT, "labels / energy is NULL");
+    Call c;
+    GINF_TRY(resolve(grid, opt, c.r));
+    WsGuard guard(wsp);
+    c.ws = guard.ws;
+    c.g = grid;
+    c.stats = nullptr;
+    GINF_TRY(ws_init(c.ws));
+    const int W = grid->width, H = grid->height, L = grid->num_labels;
+    const bool host = grid->memory == GINF_HOST;
+    const size_t ts = type_size(grid->cost_type);
+    const size_t cost_bytes = (size_t)W * H * L * ts, table_bytes = (size_t)L * L * ts;
+    const size_t lab_bytes = (size_t)W * H * sizeof(int32_t);
+    const int np = energy_num_partials(W, H);
+    Arena a;
+    const size_t id_c = host ? a.add(cost_bytes) : 0;
+    const size_t id_v = host ? a.add(table_bytes) : 0;
+    const size_t id_l = host ? a.add(lab_bytes) : 0;
+    const size_t id_p = a.add(sizeof(double) * (np + 1) + 64);
+    GINF_TRY(ws_reserve(c.ws, a.total()));
+    unsigned char *base = c.ws->arena;
+    cudaStream_t s = c.r.stream;
+    const void *costs = grid->data_costs, *V = grid->sm_costs;
+    const int32_t *lab = labels;
+    if (host) {
+        void *dc = a.ptr(base, id_c), *dv = a.ptr(base, id_v), *dl = a.ptr(base, id_l);
+        GINF_CK(cudaMemcpyAsync(dc, costs, cost_bytes, cudaMemcpyHostToDevice, s));
+        GINF_CK(cudaMemcpyAsync(dv, V, table_bytes, cudaMemcpyHostToDevice, s));
+        GINF_CK(cudaMemcpyAsync(dl, labels, lab_bytes, cudaMemcpyHostToDevice, s));
+        costs = dc;
+        V = dv;
+        lab = static_cast<const int32_t *>(dl);
+    }
+    double *partials = reinterpret_cast<double *>(a.ptr(base, id_p));
+    int *status = reinterpret_cast<int *>(partials + np);
+    double *out = partials + np + 1;
+    GINF_CK(cudaMemsetAsync(status, 0, sizeof(int), s));
+    GINF_CK(launch_energy(grid->cost_type, costs, 1, (size_t)W * H, W, H, L, V, lab, partials, np, out, status, s));
+    GINF_CK(cudaMemcpyAsync(c.ws->energy_host, out, sizeof(double), cudaMemcpyDeviceToHost, s));
+    GINF_CK(cudaMemcpyAsync(c.ws->status_host, status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GINF_CK(cudaStreamSynchronize(s));
+    if (*c.ws->status_host & DEV_ERR_BOUNDS) return fail(GINF_ERR_INVALID_ARGUMENT, "a label is outside [0, num_labels)");
+    *energy = *c.ws->energy_host;
+    return GINF_OK;
+}
+
+ginf_status ginf_solve(ginf_workspace *wsp, const ginf_grid *grid, int32_t num_levels, int32_t iters_per_level,
+                       int32_t icm_iters, int32_t *labels, double *energy, const ginf_options *opt,
+                       ginf_stats *stats) {
+    g_last_error.clear();
+    GINF_TRY(check_grid(grid));
+    if (num_levels < 1) return fail(GINF_ERR_INVALID_ARGUMENT, "num_levels must be >= 1");
+    if (iters_per_level < 0 || icm_iters < 0) return fail(GINF_ERR_INVALID_ARGUMENT, "iteration counts must be >= 0");
+    if (!labels) return fail(GINF_ERR_INVALID_ARGUMENT, "labels is NULL");
+    Call c;
+    GINF_TRY(resolve(grid, opt, c.r));
+    if (grid->num_labels > kMaxLabels)
+        return fail(GINF_ERR_UNSUPPORTED, "num_labels above " + std::to_string(kMaxLabels) + " is not compiled in");
+    WsGuard guard(wsp);
+    c.ws = guard.ws;
+    c.g = grid;
+    c.stats = stats;
+    GINF_TRY(ws_init(c.ws));
+    begin(c);
+    Prepared P;
+    const bool host = grid->memory == GINF_HOST;
+    // The caller's labels seed the device copy: ICM reads the border labels.
+    GINF_TRY(prepare(c, P, num_levels, true, host ? labels : nullptr, host ? nullptr : labels));
+    int64_t nli = 0;
+    GINF_TRY(run_bp(c, P, iters_per_level, nli));
+    GINF_TRY(run_icm_sync(c, P, icm_iters));
+    c.ev(EV_ICM);
+    GINF_TRY(run_energy(c, P));
+    c.ev(EV_ENERGY);
+    GINF_TRY(export_msgs(c, P, opt));
+    GINF_TRY(labels_to_caller(c, P, labels, true));
+    if (energy) {
+        GINF_CK(cudaMemcpyAsync(c.ws->energy_host, P.energy, sizeof(double), cudaMemcpyDeviceToHost, c.r.stream));
+        c.d2h += sizeof(double);
+    }
+    c.ev(EV_END);
+    GINF_TRY(read_status(c, P));
+    if (energy) *energy = *c.ws->energy_host;
+    return finish(c, nli);
+}
+
+ginf_status ginf_stereo_costs(int32_t width, int32_t height, int32_t num_labels, int32_t memory, const float *left,
+                              const float *right, float coef, float cap, float *costs, void *stream) {
+    g_last_error.clear();
+    if (width < 1 || height < 1 || num_labels < 1) return fail(GINF_ERR_INVALID_ARGUMENT, "bad size");
+    if (!left || !right || !costs) return fail(GINF_ERR_INVALID_ARGUMENT, "NULL buffer");
+    if (memory != GINF_HOST && memory != GINF_DEVICE) return fail(GINF_ERR_INVALID_ARGUMENT, "bad memory kind");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t img = (size_t)width * height * sizeof(float);
+    const float *l = left, *r = right;
+    float *tmp = nullptr;
+    if (memory == GINF_HOST) {
+        GINF_CK(cudaMallocAsync(&tmp, 2 * img, s));
+        GINF_CK(cudaMemcpyAsync(tmp, left, img, cudaMemcpyHostToDevice, s));
+        GINF_CK(cudaMemcpyAsync(tmp + (size_t)width * height, right, img, cudaMemcpyHostToDevice, s));
+        l = tmp;
+        r = tmp + (size_t)width * height;
+    }
+    cudaError_t e = launch_stereo_costs(width, height, num_labels, l, r, coef, cap, costs, s);
+    if (tmp) cudaFreeAsync(tmp, s);
+    if (e != cudaSuccess) return cuda_fail(e, "stereo costs");
+    GINF_CK(cudaStreamSynchronize(s));
+    return GINF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,107 @@
+// ginf_internal.h -- host/device shared declarations of the GB300 library.
+//
+// HBM layout of one pyramid level ("records"): node (x, y) owns the record at
+// rec + (y*W + x) * rec_bytes, label-contiguous:
+//
+//     [ D: Lp elements of the compute type T ][ in[0..3]: 4 x Lp elements of the store type M ]
+//
+// in[d] is the message sent TO the node BY its neighbour in direction d
+// (S=0, E=1, N=2, W=3), i.e. messages are stored at the receiver.  A node's
+// whole update input (its costs and its four incoming messages) is one
+// contiguous, 16-byte aligned block that a single bulk TMA copy brings into
+// shared memory, and each of its four outputs is one contiguous Lp-element
+// slot of a neighbour's record.  Lp is L rounded up to a multiple of 8, so
+// every slot is a whole number of 16-byte chunks for f16, f32, i32 and f64.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace ginf_gpu {
+
+enum CType { CT_F32 = 0, CT_I32 = 1, CT_F64 = 2 };
+enum Store { ST_NATIVE = 0, ST_F16 = 1 };
+enum ReadMode { RD_OWN = 0, RD_ZERO = 1, RD_COARSE = 2 };
+enum Mode { MODE_LINEAR = 0, MODE_REF_MINCONV = 1, MODE_STD_MINCONV = 2, MODE_STD_QUAD = 3 };
+
+// Device status bits (OR-ed into the workspace's status word).
+enum { DEV_ERR_TIMEOUT = 1, DEV_ERR_BOUNDS = 2 };
+
+struct LevelGeom {
+    int W = 0, H = 0;
+    size_t rec_bytes = 0;   // record stride
+    size_t offset = 0;      // byte offset of this level inside the records buffer
+};
+
+struct RecordFormat {
+    int ctype = CT_F32;     // arithmetic / cost element type in the record
+    int store = ST_NATIVE;  // message element type
+    int L = 0, Lp = 0;
+    uint32_t t_size = 4, m_size = 4;
+    uint32_t d_bytes = 0, m_bytes = 0, rec_bytes = 0, slot_bytes = 0;
+};
+
+RecordFormat make_format(int ctype, int store, int L);
+
+// Parameters of one checkerboard half-sweep launch.
+struct SweepParams {
+    int W, H, L, Lp;
+    uint32_t rec_bytes, d_bytes, m_bytes, slot_bytes;
+    unsigned char *rec;            // this level's records
+    const unsigned char *crec;     // coarser level's records (RD_COARSE)
+    int cW, cH;
+    int iter;                      // nodes with x >= ((y+iter)&1)+1, step 2, are updated
+    int read_mode;                 // ReadMode
+    int mode;                      // Mode
+    int norm_min;                  // 0 = subtract mean, 1 = subtract min
+    const void *V;                 // L*L table of the compute type (device); the
+                                   // kernel reads its slope V(0,1) and truncation
+                                   // V(0,L-1) from it, as bp.cc:35,43 do
+    int32_t *labels;               // level-0 labels (W*H) or nullptr
+    int write_labels;
+    int tiles_per_row, num_tiles;
+    int *status;
+};
+
+struct SweepConfig {
+    int nt = 32;       // nodes (threads) per tile
+    int stages = 1;    // shared-memory pipeline depth
+};
+
+// Launch one half-sweep; returns the kernel launch error.
+cudaError_t launch_sweep(const RecordFormat &f, const SweepConfig &cfg, SweepParams p, cudaStream_t s,
+                         int num_sms);
+// Largest L the sweep kernels are compiled for.
+constexpr int kMaxLabels = 128;
+bool sweep_supported(const RecordFormat &f);
+
+// Auxiliary kernels (aux_kernels.cu).
+cudaError_t launch_costs_to_records(const RecordFormat &f, int cost_type, const void *src, int W, int H,
+                                    unsigned char *rec, cudaStream_t s);
+cudaError_t launch_pyramid(const RecordFormat &f, const unsigned char *frec, int fW, int fH, unsigned char *crec,
+                           int cW, int cH, cudaStream_t s);
+cudaError_t launch_init_messages(const RecordFormat &f, unsigned char *rec, int W, int H,
+                                 const unsigned char *crec, int cW, int cH, cudaStream_t s);
+cudaError_t launch_fill_interior(int32_t *labels, int W, int H, int32_t value, cudaStream_t s);
+cudaError_t launch_decode_fresh(const RecordFormat &f, const unsigned char *rec, int W, int H, int32_t *labels,
+                                cudaStream_t s);
+cudaError_t launch_export_messages(const RecordFormat &f, const unsigned char *rec, int W, int H, void *dst,
+                                   cudaStream_t s);
+cudaError_t launch_icm_sync(const RecordFormat &f, const unsigned char *rec, int W, int H, const void *V,
+                            const int32_t *old_labels, int32_t *new_labels, int *status, cudaStream_t s);
+cudaError_t launch_icm_async_diag(const RecordFormat &f, const unsigned char *rec, int W, int H, const void *V,
+                                  int32_t *labels, int diag, int *status, cudaStream_t s);
+// Energy with costs addressed as base + node*node_stride + label*label_stride
+// (elements of the compute type): records (rec_bytes/t_size, 1) or the
+// caller's label-planar array (1, W*H).  partials holds num_partials doubles.
+cudaError_t launch_energy(int ctype, const void *costs, size_t node_stride, size_t label_stride, int W, int H, int L,
+                          const void *V, const int32_t *labels, double *partials, int num_partials, double *out,
+                          int *status, cudaStream_t s);
+int energy_num_partials(int W, int H);
+cudaError_t launch_convert_table(int src_type, int dst_type, const void *src, void *dst, int n, cudaStream_t s);
+cudaError_t launch_stereo_costs(int W, int H, int L, const float *left, const float *right, float coef, float cap,
+                                float *costs, cudaStream_t s);
+
+}  // namespace ginf_gpu

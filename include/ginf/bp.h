@@ -1,0 +1,29 @@
+// ginf/bp.h -- loopy and hierarchical min-sum belief propagation
+// (src/include/bp.h).  All four entry points run on the GPU (sm_103a) with the
+// reference CPU code's semantics (src/bp.cc): checkerboard half-sweeps over
+// interior nodes, O(L) updates for Potts / truncated-linear smoothness, and
+// the label of each interior node taken as the argmin of its belief at its
+// last update.  Interior entries of result are written, border entries keep
+// their values.  numIters counts half-sweeps (one colour each).
+#ifndef GINF_GB300_BP_H
+#define GINF_GB300_BP_H
+
+#include "core.h"
+
+namespace ginf {
+
+template <typename T>
+void decodeBp(Grid<T> *grid, int numIters, Matrix<int> *result);
+
+template <typename T>
+void gpuDecodeBp(Grid<T> *grid, int numIters, Matrix<int> *result);
+
+template <typename T>
+void decodeHbp(Grid<T> *grid, int numLevels, int numItersPerLevel, Matrix<int> *result);
+
+template <typename T>
+void gpuDecodeHbp(Grid<T> *grid, int numLevels, int numItersPerLevel, Matrix<int> *result);
+
+}  // namespace ginf
+
+#endif

@@ -1,0 +1,168 @@
+/*
+ * ginf_gb300.h -- C ABI of the GB300 (sm_103a) grid-MRF inference library.
+ *
+ * This is the drop-in boundary for GridInfCuda's inference path.  The C++
+ * entry points of the reference (namespace ginf: decodeBp / decodeHbp /
+ * gpuDecodeBp / gpuDecodeHbp, decodeIcmSync / decodeIcmAsync / gpuDecodeIcm,
+ * Grid<T>::getLabelingCost) are re-implemented on top of these functions in
+ * include/ginf/*.h; other hosts (Python ctypes, cgo, JNI ...) bind them
+ * directly.  Plain pointers and sizes only, no exceptions across the ABI,
+ * every function returns a status and never exits the process (the
+ * reference's GINF_SAFE_CALL exits, src/include/gpu.h:36-48).
+ *
+ * Data layouts are the reference's Matrix layouts (src/matrix.cc:52-56,
+ * first index fastest):
+ *   data costs   label-planar, element (x, y, l) at x + W*y + W*H*l
+ *   smoothness   L x L table, V(fp, fq) at fp + L*fq            (grid.h:22-23)
+ *   labels       int32, (x, y) at x + W*y                       (Matrix(2, W, H))
+ * Directions are S=0 (+y), E=1 (+x), N=2 (-y), W=3 (-x)         (utils.h:26-37)
+ */
+#ifndef GINF_GB300_H
+#define GINF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum ginf_status {
+    GINF_OK = 0,
+    GINF_ERR_INVALID_ARGUMENT = 1, /* bad size, null pointer, unknown enum   */
+    GINF_ERR_UNSUPPORTED = 2,      /* valid request this build does not cover */
+    GINF_ERR_CUDA = 3,             /* a CUDA runtime call or launch failed     */
+    GINF_ERR_OUT_OF_MEMORY = 4,    /* device or pinned allocation failed       */
+    GINF_ERR_TIMEOUT = 5,          /* a bounded device-side wait gave up       */
+    GINF_ERR_NO_DEVICE = 6         /* no usable sm_103 device                  */
+} ginf_status;
+
+/* Smoothness models, same numbering as ginf::SmoothnessFunctions (grid.h:9-14). */
+enum { GINF_SM_EXPLICIT = 0, GINF_SM_POTTS = 1, GINF_SM_TRUNC_LINEAR = 2, GINF_SM_TRUNC_QUAD = 3 };
+/* Cost / message arithmetic type: the reference's float and int instantiations
+ * (bp.cc:190-194), plus double for the FP64 oracle runs. */
+enum { GINF_F32 = 0, GINF_I32 = 1, GINF_F64 = 2 };
+/* Where the caller's buffers live. */
+enum { GINF_HOST = 0, GINF_DEVICE = 1 };
+/* Message rule.  REFERENCE reproduces src/bp.cc:21-63 exactly, including its
+ * O(L^2) branch for EXPLICIT and TRUNC_QUAD that neither subtracts the
+ * receiver's message nor normalises (bp.cc:55-62).  STANDARD is min-sum BP for
+ * every model: subtract, distance transform (O(L) lower envelope for
+ * TRUNC_QUAD), truncate, normalise.  The two agree for POTTS and TRUNC_LINEAR. */
+enum { GINF_RULE_REFERENCE = 0, GINF_RULE_STANDARD = 1 };
+/* Message store: the arithmetic type, or FP16 (F32 grids only; the update
+ * still runs in FP32 and messages are min-normalised so they land in
+ * [0, truncation]). */
+enum { GINF_STORE_NATIVE = 0, GINF_STORE_F16 = 1 };
+/* Final decode: STALE is the reference's argmin of each node's belief at its
+ * last update (bp.cc:65-84, 168-173); FRESH recomputes beliefs from the final
+ * messages. */
+enum { GINF_DECODE_STALE = 0, GINF_DECODE_FRESH = 1 };
+/* Message normalisation: subtract the mean (bp.cc:50-54) or the minimum. */
+enum { GINF_NORM_MEAN = 0, GINF_NORM_MIN = 1 };
+
+/* One grid MRF (the reference's ginf::Grid<T>, grid.h:16-81). */
+typedef struct ginf_grid {
+    int32_t width, height, num_labels;
+    int32_t cost_type;       /* GINF_F32 or GINF_I32 (costs are read as this type) */
+    int32_t sm_model;        /* GINF_SM_*                                         */
+    int32_t memory;          /* GINF_HOST or GINF_DEVICE, for every buffer below   */
+    const void *data_costs;  /* W*H*L elements, label-planar                      */
+    const void *sm_costs;    /* L*L elements, V(fp, fq) at fp + L*fq              */
+} ginf_grid;
+
+typedef struct ginf_options {
+    int32_t msg_rule;        /* GINF_RULE_*,   default REFERENCE            */
+    int32_t msg_store;       /* GINF_STORE_*,  default NATIVE               */
+    int32_t decode;          /* GINF_DECODE_*, default STALE                */
+    int32_t normalize;       /* GINF_NORM_*,   default MEAN (F16 uses MIN)  */
+    int32_t compute_type;    /* GINF_F32 / GINF_I32 / GINF_F64; -1 = cost_type */
+    int32_t tile_nodes;      /* nodes per sweep tile (32 or 64); 0 = tuned   */
+    int32_t stages;          /* sweep pipeline stages (1 or 2); 0 = tuned     */
+    int32_t reserved0;
+    void *stream;            /* cudaStream_t to run on; NULL = legacy default */
+    void *msgs_out;          /* optional: final level-0 messages, [H][W][4][L] of the
+                                compute type, slot d = message from the neighbour in
+                                direction d (0 where that neighbour is on the border
+                                or off the grid); same memory kind as the grid     */
+    int64_t reserved[6];
+} ginf_options;
+
+/* Per-call measurements (filled when a non-null pointer is passed; the call
+ * then synchronises its stream before returning). */
+typedef struct ginf_stats {
+    double total_ms;          /* whole call, device timeline                   */
+    double upload_ms;         /* host->device copy of costs (host grids)        */
+    double prepare_ms;        /* layout transform + pyramid                    */
+    double sweep_ms;          /* all BP half-sweeps, all levels                */
+    double level0_sweep_ms;   /* BP half-sweeps of the finest level            */
+    double icm_ms;            /* ICM sweeps                                    */
+    double energy_ms;         /* energy reduction                              */
+    double download_ms;       /* device->host copy of results                  */
+    int64_t kernel_launches;  /* kernels this call launched                    */
+    int64_t level0_sweep_launches;
+    int64_t node_label_iters; /* sum over levels of W_t*H_t*L*iterations       */
+    int64_t h2d_bytes, d2h_bytes;
+} ginf_stats;
+
+typedef struct ginf_workspace ginf_workspace;
+
+/* Library information and errors. */
+const char *ginf_version(void);
+/* Message of the last failing call on this host thread ("" if none). */
+const char *ginf_last_error(void);
+void ginf_default_options(ginf_options *opt);
+
+/* Reusable device buffers and events; one per host thread or stream.
+ * Passing NULL to the solver entry points allocates and frees per call, as
+ * the reference does (src/gpu/bp.cu:141-222). */
+ginf_status ginf_workspace_create(ginf_workspace **ws);
+ginf_status ginf_workspace_destroy(ginf_workspace *ws);
+
+/* Hierarchical min-sum BP, num_levels == 1 being loopy BP.
+ * Replaces ginf::decodeHbp (src/bp.cc:86-180), ginf::decodeBp (bp.cc:182-187),
+ * ginf::gpuDecodeHbp (src/gpu/bp.cu:133-223) and ginf::gpuDecodeBp
+ * (bp.cu:228-231), with the CPU code's semantics.  labels is W*H int32 in the
+ * grid's memory kind; interior entries are written, border entries are left
+ * as the caller set them (bp.cc:169-173). */
+ginf_status ginf_decode_hbp(ginf_workspace *ws, const ginf_grid *grid, int32_t num_levels,
+                            int32_t iters_per_level, int32_t *labels, const ginf_options *opt,
+                            ginf_stats *stats);
+
+/* ICM.  asynchronous == 0: Jacobi sweeps, replacing ginf::decodeIcmSync
+ * (src/icm.cc:4-38) and ginf::gpuDecodeIcm (src/gpu/icm.cu:53-83).
+ * asynchronous == 1: raster-order Gauss-Seidel, replacing ginf::decodeIcmAsync
+ * (src/icm.cc:40-67), run as an exact anti-diagonal wavefront.
+ * result (W*H) receives a copy of initial, then interior nodes are updated. */
+ginf_status ginf_decode_icm(ginf_workspace *ws, const ginf_grid *grid, const int32_t *initial,
+                            int32_t iters, int32_t asynchronous, int32_t *result,
+                            const ginf_options *opt, ginf_stats *stats);
+
+/* Energy of a labelling, ginf::Grid<T>::getLabelingCost(Matrix<int>*)
+ * (src/grid.cc:102-125): interior nodes' data terms plus their N and E edges,
+ * summed in FP64 on the device (deterministic order). */
+ginf_status ginf_energy(ginf_workspace *ws, const ginf_grid *grid, const int32_t *labels,
+                        double *energy, const ginf_options *opt);
+
+/* HBP, then ICM refinement, then the FP64 energy, with one upload of the
+ * costs: decodeHbp (bp.cc:86-180) + decodeIcmSync (icm.cc:4-38) +
+ * getLabelingCost (grid.cc:102-125) in one call.  labels receives the refined
+ * labelling (border entries keep the caller's values), energy may be NULL. */
+ginf_status ginf_solve(ginf_workspace *ws, const ginf_grid *grid, int32_t num_levels,
+                       int32_t iters_per_level, int32_t icm_iters, int32_t *labels, double *energy,
+                       const ginf_options *opt, ginf_stats *stats);
+
+/* Stereo data costs on the device: D(x, y, d) = coef * min(|left(x,y) -
+ * right(max(x-d, 0), y)|, cap) for d < L, label-planar float32 into costs
+ * (device memory, W*H*L).  left / right are W*H float32 images in the memory
+ * kind given.  The GPU form of the cost loop in
+ * examples/stereo/stereo.cc:28-34 (with x-d clamped at 0 instead of zero-cost
+ * columns). */
+ginf_status ginf_stereo_costs(int32_t width, int32_t height, int32_t num_labels, int32_t memory,
+                              const float *left, const float *right, float coef, float cap,
+                              float *costs, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GINF_GB300_H */

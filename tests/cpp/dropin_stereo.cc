@@ -1,0 +1,56 @@
+// A program written against the GridInfCuda C++ API (the shape of
+// examples/stereo/stereo.cc: Grid<int>, truncated-linear smoothness, loopy BP),
+// here on a seeded synthetic stereo pair read from a raw file instead of
+// OpenCV images.  It exercises the drop-in headers include/ginf/*.h.
+//
+//   dropin_stereo <in.raw> <out.raw>
+//   in.raw : int32 W, H, L, then W*H*L int32 costs (label-planar)
+//   out.raw: int32 W*H labels of gpuDecodeBp (30 iterations), then
+//            W*H labels of decodeHbp (3 levels x 6), then W*H labels of
+//            decodeIcmSync (2 sweeps from the BP labels), then the
+//            energy of the BP labelling as int32.
+#include <cstdio>
+#include <vector>
+
+#include "ginf/bp.h"
+#include "ginf/core.h"
+#include "ginf/icm.h"
+
+int main(int argc, char **argv) {
+    if (argc != 3) {
+        std::fprintf(stderr, "usage: %s in.raw out.raw\n", argv[0]);
+        return 2;
+    }
+    FILE *f = std::fopen(argv[1], "rb");
+    if (!f) return 2;
+    int hdr[3];
+    if (std::fread(hdr, sizeof(int), 3, f) != 3) return 2;
+    const int W = hdr[0], H = hdr[1], L = hdr[2];
+    ginf::Grid<int> grid(W, H, L);
+    std::vector<int> costs((size_t)W * H * L);
+    if (std::fread(costs.data(), sizeof(int), costs.size(), f) != costs.size()) return 2;
+    std::fclose(f);
+    for (int k = 0; k < L; k++)
+        for (int y = 0; y < H; y++)
+            for (int x = 0; x < W; x++) grid.setDataCost(x, y, k, costs[(size_t)x + (size_t)W * y + (size_t)W * H * k]);
+    grid.useSmoothnessTruncLinear(10, 20);
+
+    ginf::Matrix<int> bp(2, W, H), hbp(2, W, H), icm(2, W, H);
+    ginf::gpuDecodeBp(&grid, 30, &bp);
+    if (ginf::lastStatus() != 0) return 1;
+    ginf::decodeHbp(&grid, 3, 6, &hbp);
+    if (ginf::lastStatus() != 0) return 1;
+    ginf::decodeIcmSync(&grid, &bp, 2, &icm);
+    if (ginf::lastStatus() != 0) return 1;
+    const int energy = grid.getLabelingCost(&bp);
+    if (ginf::lastStatus() != 0) return 1;
+
+    FILE *o = std::fopen(argv[2], "wb");
+    if (!o) return 2;
+    std::fwrite(bp.data, sizeof(int), (size_t)W * H, o);
+    std::fwrite(hbp.data, sizeof(int), (size_t)W * H, o);
+    std::fwrite(icm.data, sizeof(int), (size_t)W * H, o);
+    std::fwrite(&energy, sizeof(int), 1, o);
+    std::fclose(o);
+    return 0;
+}

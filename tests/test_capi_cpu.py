@@ -1,0 +1,88 @@
+"""The C-ABI library without a GPU: it loads, exports every symbol the public
+headers declare, and rejects bad arguments before touching a device."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+
+def _declared_c_functions():
+    hdr = open(os.path.join(ROOT, "include", "ginf_gb300.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    return sorted(set(re.findall(r"\b(ginf_[a-z0-9_]+)\s*\(", hdr)))
+
+
+def test_every_c_abi_symbol_is_exported(built_lib):
+    names = _declared_c_functions()
+    assert len(names) >= 10
+    lib = ctypes.CDLL(built_lib)
+    out = subprocess.run(["nm", "-D", "--defined-only", built_lib], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in exported, n
+
+
+CXX_SIGNATURES = [
+    "ginf::decodeBp<float>(ginf::Grid<float>*, int, ginf::Matrix<int>*)",
+    "ginf::decodeBp<int>(ginf::Grid<int>*, int, ginf::Matrix<int>*)",
+    "ginf::gpuDecodeBp<float>(ginf::Grid<float>*, int, ginf::Matrix<int>*)",
+    "ginf::decodeHbp<float>(ginf::Grid<float>*, int, int, ginf::Matrix<int>*)",
+    "ginf::decodeHbp<int>(ginf::Grid<int>*, int, int, ginf::Matrix<int>*)",
+    "ginf::gpuDecodeHbp<int>(ginf::Grid<int>*, int, int, ginf::Matrix<int>*)",
+    "ginf::decodeIcmSync<float>(ginf::Grid<float>*, ginf::Matrix<int>*, int, ginf::Matrix<int>*)",
+    "ginf::decodeIcmAsync<int>(ginf::Grid<int>*, ginf::Matrix<int>*, int, ginf::Matrix<int>*)",
+    "ginf::gpuDecodeIcm<float>(ginf::Grid<float>*, ginf::Matrix<int>*, int, ginf::Matrix<int>*)",
+    "ginf::Grid<float>::getLabelingCost(ginf::Matrix<int>*)",
+    "ginf::Grid<int>::useSmoothnessTruncLinear(int, int)",
+    "ginf::Grid<float>::useSmoothnessTruncQuad(float, float)",
+    "ginf::Grid<float>::setSmoothnessCost(int, int, float)",
+    "ginf::Matrix<int>::Matrix(int, ...)",
+    "ginf::Matrix<float>::copyFrom(ginf::Matrix<float>*)",
+    "ginf::lastStatus()",
+]
+
+
+def test_cpp_api_symbols_are_exported(built_lib):
+    out = subprocess.run(["nm", "-DC", "--defined-only", built_lib], capture_output=True, text=True).stdout
+    for sig in CXX_SIGNATURES:
+        assert sig in out, sig
+
+
+def test_cpp_dropin_program_compiles_against_headers(built_lib, tmp_path):
+    """The drop-in example builds against include/ginf and links the library."""
+    exe = tmp_path / "dropin"
+    r = subprocess.run(["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", "dropin_stereo.cc"), "-o", str(exe),
+                        built_lib, "-Wl,-rpath," + os.path.dirname(built_lib)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_argument_validation_without_device(built_lib):
+    from gridinfcuda_gb300 import capi
+    L = capi.lib()
+    assert L.ginf_decode_hbp(None, None, 1, 1, None, None, None) == capi.ERR_INVALID_ARGUMENT
+    assert b"NULL" in L.ginf_last_error()
+    import numpy as np
+    D = np.zeros((1, 4, 4), np.float32)
+    V = np.zeros(1, np.float32)
+    g = capi.Grid(4, 4, 1, capi.F32, capi.TRUNC_LINEAR, capi.HOST, D.ctypes.data, V.ctypes.data)
+    lab = np.zeros((4, 4), np.int32)
+    assert L.ginf_decode_hbp(None, ctypes.byref(g), 1, 1, lab.ctypes.data, None, None) == capi.ERR_INVALID_ARGUMENT
+    g.num_labels, g.sm_model = 4, 9
+    assert L.ginf_decode_hbp(None, ctypes.byref(g), 1, 1, lab.ctypes.data, None, None) == capi.ERR_INVALID_ARGUMENT
+    assert b"model" in L.ginf_last_error()
+
+
+def test_default_options_layout(built_lib):
+    from gridinfcuda_gb300 import capi
+    o = capi.options()
+    assert (o.msg_rule, o.msg_store, o.decode, o.normalize, o.compute_type) == (0, 0, 0, 0, -1)
+    assert ctypes.sizeof(capi.Options) == 8 * 4 + 2 * 8 + 6 * 8
+    assert ctypes.sizeof(capi.Grid) == 6 * 4 + 2 * 8
+    assert ctypes.sizeof(capi.Stats) == 8 * 8 + 5 * 8
+    assert capi.version().startswith("gridinfcuda-gb300")

@@ -1,0 +1,41 @@
+"""The C++ drop-in API (include/ginf/*.h) on the GPU: a program written the
+way the reference example is written, compared with the oracle."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from gridinfcuda_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def test_cpp_program_matches_oracle(ginf, orc, built_lib, tmp_path):
+    exe = tmp_path / "dropin"
+    r = subprocess.run(["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", "dropin_stereo.cc"), "-o", str(exe), built_lib,
+                        "-Wl,-rpath," + os.path.dirname(built_lib)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    W, H, L = 120, 90, 16
+    pair = synth.stereo_pair(W, H, L, 8, 2.0, seed=17)
+    D = np.minimum(np.abs(np.rint(pair.left)[None].astype(np.int32) -
+                          np.stack([np.rint(pair.right[:, np.maximum(np.arange(W) - k, 0)]).astype(np.int32)
+                                    for k in range(L)])), 20).astype(np.int32)
+    inp, out = tmp_path / "in.raw", tmp_path / "out.raw"
+    with open(inp, "wb") as f:
+        np.array([W, H, L], np.int32).tofile(f)
+        D.tofile(f)
+    r = subprocess.run([str(exe), str(inp), str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    res = np.fromfile(out, np.int32)
+    n = W * H
+    bp, hbp, icm, energy = res[:n].reshape(H, W), res[n:2 * n].reshape(H, W), res[2 * n:3 * n].reshape(H, W), res[-1]
+    V = synth.sm_table(L, synth.TRUNC_LINEAR, 10, 20, dtype=np.int32)
+    want_bp, _ = orc.hbp(D, V, synth.TRUNC_LINEAR, 1, 30)
+    want_hbp, _ = orc.hbp(D, V, synth.TRUNC_LINEAR, 3, 6)
+    assert np.array_equal(bp, want_bp)
+    assert np.array_equal(hbp, want_hbp)
+    assert np.array_equal(icm, orc.icm(D, V, want_bp, 2))
+    assert energy == orc.energy(D, V, want_bp, exact_type=True)

@@ -1,0 +1,234 @@
+"""GPU parity: the CUDA path, called through the C ABI, against the reference's
+own outputs (golden fixtures) and the CPU oracle.  FP32 and int32 BP, HBP and
+ICM are required to be bit-identical; FP16 / FP64 / standard-rule runs are
+held to the tolerances written in each test."""
+import numpy as np
+import pytest
+
+from gridinfcuda_gb300 import synth
+from helpers import golden_problem, sha, workload
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _cases(meta, kind):
+    return [(n, c) for n, c in meta["cases"].items() if c["kind"] == kind]
+
+
+def test_golden_bp_cases_bit_exact(ginf, golden):
+    meta, arr = golden
+    for name, case in _cases(meta, "bp"):
+        P = golden_problem(case)
+        init = arr[name + "/init"].astype(np.int32)
+        lab, msgs = ginf.decode_hbp(P.D, P.V, case["model"], 1, case["iters"], labels=init.copy(), want_msgs=True)
+        assert np.array_equal(lab, arr[name + "/labels"]), name
+        if "msgs_sha" in case:
+            assert sha(msgs) == case["msgs_sha"], name
+        else:
+            assert np.array_equal(msgs.view(np.uint32), arr[name + "/msgs"].view(np.uint32)), name
+        icm_s = ginf.decode_icm(P.D, P.V, case["model"], lab, 3)
+        assert np.array_equal(icm_s, arr[name + "/icm_sync3"]), name
+        icm_a = ginf.decode_icm(P.D, P.V, case["model"], lab, 2, asynchronous=True)
+        assert np.array_equal(icm_a, arr[name + "/icm_async2"]), name
+        e = ginf.energy(P.D, P.V, case["model"], lab)
+        assert e == pytest.approx(case["energy_ref_type"], rel=1e-5, abs=1e-6), name
+
+
+def test_golden_hbp_cases_bit_exact(ginf, golden):
+    meta, arr = golden
+    for name, case in _cases(meta, "hbp"):
+        P = golden_problem(case)
+        init = arr[name + "/init"].astype(np.int32)
+        lab = ginf.decode_hbp(P.D, P.V, case["model"], case["levels"], case["iters"], labels=init.copy())
+        assert np.array_equal(lab, arr[name + "/labels"]), name
+
+
+def test_golden_cases_device_buffers(ginf, golden):
+    """Same fixtures with every buffer resident on the device."""
+    meta, arr = golden
+    for name, case in meta["cases"].items():
+        if case["kind"] not in ("bp", "hbp"):
+            continue
+        P = golden_problem(case)
+        init = _dev(arr[name + "/init"].astype(np.int32))
+        lab = ginf.decode_hbp(_dev(P.D), _dev(P.V), case["model"], case["levels"], case["iters"], labels=init)
+        assert np.array_equal(lab.cpu().numpy(), arr[name + "/labels"]), name
+
+
+def test_plain_bp_workload_matches_reference(ginf, golden):
+    meta, _ = golden
+    case = meta["cases"]["plain_bp_384x288_L16"]
+    P = workload("plain_bp")
+    assert sha(P.D) == case["cost_sha"]
+    lab = ginf.decode_hbp(P.D, P.V, P.model, 1, 50)
+    assert sha(lab) == case["labels_sha"]
+    assert ginf.energy(P.D, P.V, P.model, lab) == pytest.approx(case["energy_f64"], rel=1e-12)
+    icm = ginf.decode_icm(P.D, P.V, P.model, lab, 5)
+    assert sha(icm) == case["icm5_sha"]
+
+
+def test_hbp_workload_matches_reference(ginf, golden):
+    """1920x1080, L=64, 5 levels x 10 half-sweeps, 5 ICM sweeps: labels
+    bit-identical to the reference CPU code, energy in FP64."""
+    meta, _ = golden
+    case = meta["cases"].get("hbp_1920x1080_L64")
+    if case is None:
+        pytest.skip("large golden case not generated")
+    P = workload("hbp_1920")
+    assert sha(P.D) == case["cost_sha"]
+    lab = ginf.decode_hbp(P.D, P.V, P.model, 5, 10)
+    assert sha(lab) == case["labels_sha"]
+    lab2, e = ginf.solve(_dev(P.D), _dev(P.V), P.model, 5, 10, 5)
+    assert sha(lab2.cpu().numpy()) == case["icm5_sha"]
+    assert e == pytest.approx(case["icm5_energy_f64"], rel=1e-12)
+
+
+@pytest.mark.parametrize("W,H,L,levels,iters", [
+    (5, 5, 2, 1, 4), (8, 3, 5, 1, 6), (47, 35, 33, 1, 7), (50, 40, 65, 2, 5), (39, 27, 100, 1, 5),
+    (64, 64, 128, 3, 4), (129, 97, 16, 4, 6), (200, 3, 16, 1, 5), (3, 200, 32, 2, 5), (70, 50, 64, 1, 2)])
+def test_random_vs_oracle(ginf, orc, W, H, L, levels, iters):
+    P = synth.random_problem(W, H, L, W * 131 + H * 7 + L)
+    want, msgs_want = orc.hbp(P.D, P.V, P.model, levels, iters, want_msgs=True)
+    for tile, stages in ((0, 0), (32, 2), (64, 1)):
+        got, msgs = ginf.decode_hbp(P.D, P.V, P.model, levels, iters, want_msgs=True, tile_nodes=tile, stages=stages)
+        assert np.array_equal(got[1:-1, 1:-1], want[1:-1, 1:-1]), (tile, stages)
+        assert np.array_equal(msgs.view(np.uint32), msgs_want.view(np.uint32)), (tile, stages)
+
+
+def test_int_grid_vs_oracle(ginf, orc):
+    P = synth.random_problem(61, 45, 16, 77, dtype=np.int32, scale=10, trunc=20, cost_max=40)
+    want, mw = orc.hbp(P.D, P.V, P.model, 3, 6, want_msgs=True)
+    got, mg = ginf.decode_hbp(P.D, P.V, P.model, 3, 6, want_msgs=True)
+    assert np.array_equal(got, want)
+    assert np.array_equal(mg, mw)
+
+
+def test_reference_rule_quadratic_and_explicit(ginf, orc):
+    for model in (synth.TRUNC_QUAD, synth.EXPLICIT):
+        P = synth.random_problem(37, 29, 12, 5 + model, model=model, scale=1.0, trunc=9.0)
+        want, mw = orc.hbp(P.D, P.V, model, 1, 4, want_msgs=True)
+        got, mg = ginf.decode_hbp(P.D, P.V, model, 1, 4, want_msgs=True)
+        assert np.array_equal(got, want)
+        assert np.array_equal(mg.view(np.uint32), mw.view(np.uint32))
+
+
+def _renorm(m):
+    m = m.astype(np.float64)
+    return m - m.mean(axis=-1, keepdims=True)
+
+
+def _msg_rel_err(a, b):
+    """max |a-b| / max|b| after re-normalising both to zero mean per message."""
+    a, b = _renorm(a), _renorm(b)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-30)
+
+
+def test_fp64_path_matches_fp64_oracle(ginf, orc):
+    P = synth.random_problem(45, 33, 24, 31, model=synth.TRUNC_QUAD, scale=0.5, trunc=9.0)
+    want, mw = orc.hbp_f64_std(P.D, P.V, P.model, 2, 6, want_msgs=True)
+    got, mg = ginf.decode_hbp(P.D, P.V, P.model, 2, 6, want_msgs=True, compute_type=ginf.F64, rule=ginf.RULE_STANDARD)
+    assert _msg_rel_err(mg, mw) < 1e-12
+    assert (got[1:-1, 1:-1] == want[1:-1, 1:-1]).mean() == 1.0
+
+
+def test_standard_quadratic_fp32_and_fp16_vs_fp64_oracle(ginf, orc):
+    """Truncated-quadratic standard BP (O(L) lower envelope): FP32 store within
+    1e-4 relative of the FP64 oracle, FP16 store within 5e-3; labels agree on
+    >= 99.9% (FP32) and >= 99% (FP16) of nodes; energies within 1e-5 / 1e-3."""
+    P = synth.stereo_problem(96, 72, 32, seed=4, n_regions=10, sigma=3.0, planar=True, coef=0.05, cap=20.0,
+                             model=synth.TRUNC_QUAD, scale=1.0, trunc=25.0)
+    want, mw = orc.hbp_f64_std(P.D, P.V, P.model, 1, 12, want_msgs=True)
+    e_want = orc.energy(P.D, P.V, want)
+    f32, m32 = ginf.decode_hbp(P.D, P.V, P.model, 1, 12, want_msgs=True, rule=ginf.RULE_STANDARD)
+    assert _msg_rel_err(m32, mw) < 1e-4
+    assert (f32[1:-1, 1:-1] == want[1:-1, 1:-1]).mean() >= 0.999
+    assert abs(orc.energy(P.D, P.V, f32) - e_want) / abs(e_want) < 1e-5
+    _, mw_min = orc.hbp_f64_std(P.D, P.V, P.model, 1, 12, norm=1, want_msgs=True)
+    f16, m16 = ginf.decode_hbp(P.D, P.V, P.model, 1, 12, want_msgs=True, rule=ginf.RULE_STANDARD,
+                               store=ginf.STORE_F16)
+    assert _msg_rel_err(m16, mw_min) < 5e-3
+    assert (f16[1:-1, 1:-1] == want[1:-1, 1:-1]).mean() >= 0.99
+    assert abs(orc.energy(P.D, P.V, f16) - e_want) / abs(e_want) < 1e-3
+
+
+def test_fp16_store_linear_vs_fp64(ginf, orc):
+    P = synth.workload_plain_bp()
+    want, _ = orc.hbp_f64_std(P.D, P.V, P.model, 1, 50)
+    got = ginf.decode_hbp(P.D, P.V, P.model, 1, 50, store=ginf.STORE_F16)
+    assert (got[1:-1, 1:-1] == want[1:-1, 1:-1]).mean() >= 0.99
+    e_w, e_g = orc.energy(P.D, P.V, want), orc.energy(P.D, P.V, got)
+    assert abs(e_g - e_w) / abs(e_w) < 1e-3
+
+
+def test_fresh_decode_vs_oracle(ginf, orc):
+    P = synth.random_problem(52, 40, 16, 3)
+    want, _ = orc.hbp_f64_std(P.D, P.V, P.model, 1, 10, decode=1)
+    got = ginf.decode_hbp(P.D, P.V, P.model, 1, 10, decode=ginf.DECODE_FRESH)
+    assert (got[1:-1, 1:-1] == want[1:-1, 1:-1]).mean() > 0.99
+
+
+def test_deterministic_and_workspace_reuse(ginf):
+    P = synth.random_problem(90, 70, 32, 8)
+    with ginf.Workspace() as ws:
+        a, ma = ginf.decode_hbp(P.D, P.V, P.model, 3, 6, want_msgs=True, workspace=ws)
+        b, mb = ginf.decode_hbp(P.D, P.V, P.model, 3, 6, want_msgs=True, workspace=ws)
+        small = synth.random_problem(20, 10, 8, 2)
+        ginf.decode_hbp(small.D, small.V, small.model, 1, 3, workspace=ws)
+        c, mc = ginf.decode_hbp(P.D, P.V, P.model, 3, 6, want_msgs=True, workspace=ws)
+    assert np.array_equal(a, b) and np.array_equal(a, c)
+    assert np.array_equal(ma.view(np.uint32), mb.view(np.uint32))
+    assert np.array_equal(ma.view(np.uint32), mc.view(np.uint32))
+
+
+def test_solve_matches_separate_calls(ginf, orc):
+    P = synth.random_problem(80, 60, 32, 21)
+    lab, e = ginf.solve(P.D, P.V, P.model, 3, 6, 4)
+    hbp, _ = orc.hbp(P.D, P.V, P.model, 3, 6)
+    icm = orc.icm(P.D, P.V, hbp, 4)
+    assert np.array_equal(lab, icm)
+    assert e == pytest.approx(orc.energy(P.D, P.V, icm), rel=1e-12)
+
+
+def test_border_labels_untouched(ginf):
+    P = synth.random_problem(30, 20, 8, 4)
+    init = np.full((20, 30), 7, np.int32)
+    lab = ginf.decode_hbp(P.D, P.V, P.model, 2, 4, labels=init)
+    assert (lab[0] == 7).all() and (lab[-1] == 7).all() and (lab[:, 0] == 7).all() and (lab[:, -1] == 7).all()
+
+
+def test_stereo_cost_kernel_bit_exact(ginf):
+    import torch
+    pair = synth.stereo_pair(160, 90, 24, 5, 2.0, seed=3)
+    want = synth.cost_volume(pair, 24, 0.07, 15.0)
+    out = torch.empty((24, 90, 160), dtype=torch.float32, device="cuda")
+    ginf.stereo_costs(_dev(pair.left), _dev(pair.right), 24, 0.07, 15.0, out)
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), want.view(np.uint32))
+    out2 = torch.empty_like(out)
+    ginf.stereo_costs(pair.left, pair.right, 24, 0.07, 15.0, out2)
+    assert torch.equal(out, out2)
+
+
+def test_errors_are_reported_not_fatal(ginf):
+    P = synth.random_problem(10, 8, 4, 1)
+    with pytest.raises(ginf.GinfError) as e:
+        ginf.decode_hbp(P.D, P.V, P.model, 0, 3)
+    assert e.value.status == ginf.ERR_INVALID_ARGUMENT
+    big = synth.random_problem(6, 5, 130, 1)
+    with pytest.raises(ginf.GinfError) as e:
+        ginf.decode_hbp(big.D, big.V, big.model, 1, 3)
+    assert e.value.status == ginf.ERR_UNSUPPORTED
+    bad = np.full((8, 10), 9, np.int32)   # labels outside [0, 4)
+    with pytest.raises(ginf.GinfError) as e:
+        ginf.energy(P.D, P.V, P.model, bad)
+    assert e.value.status == ginf.ERR_INVALID_ARGUMENT
+    with pytest.raises(ginf.GinfError) as e:
+        ginf.decode_icm(P.D, P.V, P.model, bad, 2)
+    assert e.value.status == ginf.ERR_INVALID_ARGUMENT
+    # the library stays usable after the errors
+    lab = ginf.decode_hbp(P.D, P.V, P.model, 1, 3)
+    assert lab.shape == (8, 10)

@@ -1,0 +1,199 @@
+"""The CPU oracle against the reference's own compiled code and the golden
+fixtures that code produced (CPU only)."""
+import numpy as np
+import pytest
+
+from gridinfcuda_gb300 import synth
+from helpers import golden_problem, sha, workload
+
+
+def _need_ref(orc):
+    if orc.ref() is None:
+        pytest.skip("reference checkout not present: the golden fixtures stand in for it")
+
+
+@pytest.mark.parametrize("model,scale,d", [(synth.POTTS, 0.7, 0.0), (synth.TRUNC_LINEAR, 1.0, 1.7),
+                                           (synth.TRUNC_QUAD, 1.0, 25.0), (synth.TRUNC_LINEAR, 2.5, 3.0)])
+def test_tables_match_reference(orc, model, scale, d):
+    _need_ref(orc)
+    for L in (2, 3, 16, 17, 64, 128):
+        mine = synth.sm_table(L, model, scale, d)
+        ref = orc.ref_table(L, model, scale, d)
+        assert np.array_equal(mine.view(np.uint32), ref.view(np.uint32))
+
+
+@pytest.mark.parametrize("W,H,L,seed,model", [(17, 13, 16, 100, 2), (9, 7, 3, 101, 2), (31, 23, 17, 102, 1),
+                                               (12, 10, 8, 103, 3), (11, 9, 5, 104, 0), (2, 6, 4, 105, 2)])
+def test_oracle_vs_reference(orc, W, H, L, seed, model):
+    _need_ref(orc)
+    P = synth.random_problem(W, H, L, seed, model=model, scale=0.8 if model == 1 else 1.0,
+                             trunc=4.0 if model == 3 else 1.7)
+    init = np.full((H, W), 5 % L, np.int32)
+    for levels, iters in [(1, 0), (1, 1), (1, 2), (1, 7), (2, 3), (3, 5)]:
+        mine, _ = orc.hbp(P.D, P.V, model, levels, iters, labels=init)
+        ref = orc.ref_hbp(P.D, P.V, model, P.scale, P.trunc, levels, iters, labels=init)
+        assert np.array_equal(mine, ref), (levels, iters)
+    if model != synth.EXPLICIT:
+        _, m = orc.hbp(P.D, P.V, model, 1, 9, want_msgs=True)
+        r = orc.ref_bp_msgs(P.D, P.V, model, P.scale, P.trunc, 9)
+        assert np.array_equal(m.view(np.uint32), r.view(np.uint32))
+    for asyn in (False, True):
+        assert np.array_equal(orc.icm(P.D, P.V, mine, 3, asynchronous=asyn),
+                              orc.ref_icm(P.D, P.V, model, P.scale, P.trunc, mine, 3, asynchronous=asyn))
+    assert np.float32(orc.energy(P.D, P.V, mine, exact_type=True)) == \
+        np.float32(orc.ref_energy(P.D, P.V, model, P.scale, P.trunc, mine))
+
+
+def test_oracle_stereo_png_vs_reference(orc):
+    """Real data: the reference example's stereo pair (stereo.cc:28-45 recipe:
+    Grid<int>, L=16, cost min(|L - R(x-k)|, 20) for x >= L-1, TruncLinear(10, 20),
+    30 iterations), decoded by the oracle and by the reference."""
+    _need_ref(orc)
+    import os
+    import struct
+    import zlib
+    path = "/root/reference/examples/stereo"
+
+    def gray(png):
+        data = open(png, "rb").read()
+        w, h, depth, ctype = struct.unpack(">IIBB", data[16:26])
+        chunks, pos = b"", 8
+        while pos < len(data):
+            n = struct.unpack(">I", data[pos:pos + 4])[0]
+            if data[pos + 4:pos + 8] == b"IDAT":
+                chunks += data[pos + 8:pos + 8 + n]
+            pos += 12 + n
+        raw = zlib.decompress(chunks)
+        ch = {0: 1, 2: 3, 6: 4}[ctype]
+        stride = w * ch
+        out = np.zeros((h, stride), np.int64)
+        prev = np.zeros(stride, np.int64)
+        for y in range(h):
+            f = raw[y * (stride + 1)]
+            line = np.frombuffer(raw[y * (stride + 1) + 1:(y + 1) * (stride + 1)], np.uint8).astype(np.int64)
+            cur = np.zeros(stride, np.int64)
+            for x in range(stride):
+                a = cur[x - ch] if x >= ch else 0
+                b = prev[x]
+                c = prev[x - ch] if x >= ch else 0
+                if f == 0: p = 0
+                elif f == 1: p = a
+                elif f == 2: p = b
+                elif f == 3: p = (a + b) // 2
+                else:
+                    pa, pb, pc = abs(b - c), abs(a - c), abs(a + b - 2 * c)
+                    p = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+                cur[x] = (line[x] + p) & 255
+            out[y] = cur
+            prev = cur
+        px = out.reshape(h, w, ch)
+        if ch == 1:
+            return px[:, :, 0]
+        r, g, b = px[:, :, 0], px[:, :, 1], px[:, :, 2]
+        return (r * 299 + g * 587 + b * 114 + 500) // 1000   # luma; any fixed grey map serves as test data
+    if not os.path.exists(os.path.join(path, "left.png")):
+        pytest.skip("stereo pair not present")
+    left, right = gray(os.path.join(path, "left.png")), gray(os.path.join(path, "right.png"))
+    H, W = left.shape
+    L = 16
+    D = np.zeros((L, H, W), np.int32)
+    for k in range(L):
+        D[k, :, L - 1:] = np.minimum(np.abs(left[:, L - 1:] - right[:, L - 1 - k:W - k]), 20)
+    V = synth.sm_table(L, synth.TRUNC_LINEAR, 10, 20, dtype=np.int32)
+    mine, _ = orc.hbp(D, V, synth.TRUNC_LINEAR, 1, 30)
+    ref = orc.ref_hbp(D, V, synth.TRUNC_LINEAR, 10, 20, 1, 30)
+    assert np.array_equal(mine, ref)
+
+
+def test_oracle_matches_golden_small(orc, golden):
+    meta, arr = golden
+    for name, case in meta["cases"].items():
+        if case["kind"] not in ("bp", "hbp"):
+            continue
+        P = golden_problem(case)
+        assert sha(P.D) == case["cost_sha"], f"{name}: synthetic generator drifted"
+        init = arr[name + "/init"].astype(np.int32)
+        lab, msgs = orc.hbp(P.D, P.V, case["model"], case["levels"], case["iters"], labels=init,
+                            want_msgs=case["kind"] == "bp")
+        assert np.array_equal(lab, arr[name + "/labels"]), name
+        if case["kind"] == "bp":
+            if "msgs_sha" in case:
+                assert sha(msgs) == case["msgs_sha"], name
+            else:
+                assert np.array_equal(msgs.view(np.uint32), arr[name + "/msgs"].view(np.uint32)), name
+            assert np.array_equal(orc.icm(P.D, P.V, lab, 3), arr[name + "/icm_sync3"]), name
+            assert np.array_equal(orc.icm(P.D, P.V, lab, 2, asynchronous=True), arr[name + "/icm_async2"]), name
+        e = orc.energy(P.D, P.V, lab, exact_type=True)
+        assert np.float32(e) == np.float32(case["energy_ref_type"]), name
+
+
+def test_oracle_matches_golden_plain_bp(orc, golden):
+    meta, arr = golden
+    case = meta["cases"]["plain_bp_384x288_L16"]
+    P = workload("plain_bp")
+    assert sha(P.D) == case["cost_sha"]
+    lab, _ = orc.hbp(P.D, P.V, P.model, 1, 50)
+    assert sha(lab) == case["labels_sha"]
+    assert orc.energy(P.D, P.V, lab) == pytest.approx(case["energy_f64"], rel=1e-12)
+    icm = orc.icm(P.D, P.V, lab, 5)
+    assert sha(icm) == case["icm5_sha"]
+
+
+def test_oracle_matches_golden_hbp_full(orc, golden):
+    meta, _ = golden
+    case = meta["cases"].get("hbp_1920x1080_L64")
+    if case is None:
+        pytest.skip("large golden case not generated")
+    P = workload("hbp_1920")
+    assert sha(P.D) == case["cost_sha"]
+    lab, _ = orc.hbp(P.D, P.V, P.model, 5, 10)
+    assert sha(lab) == case["labels_sha"]
+    icm = orc.icm(P.D, P.V, lab, 5)
+    assert sha(icm) == case["icm5_sha"]
+    assert orc.energy(P.D, P.V, icm) == pytest.approx(case["icm5_energy_f64"], rel=1e-12)
+
+
+def test_oracle_thread_count_invariant(orc):
+    P = synth.random_problem(57, 41, 16, 7)
+    a, ma = orc.hbp(P.D, P.V, P.model, 2, 6, want_msgs=True, nthreads=1)
+    b, mb = orc.hbp(P.D, P.V, P.model, 2, 6, want_msgs=True, nthreads=4)
+    assert np.array_equal(a, b) and np.array_equal(ma.view(np.uint32), mb.view(np.uint32))
+
+
+def test_dt_quad_matches_brute_force(orc):
+    rng = synth.Rng(5, 3)
+    for L in (2, 3, 8, 17, 64, 128):
+        for s in (0.25, 1.0, 3.0):
+            f = rng.uniform(L) * 50.0
+            i = np.arange(L)
+            V = s * (i[None, :] - i[:, None]).astype(np.float64) ** 2
+            brute = orc.minconv_brute(f, V.reshape(-1))
+            assert np.allclose(orc.dt_quad(f, s), brute, rtol=0, atol=1e-9), (L, s)
+
+
+def test_pyramid_ceil_halving(orc):
+    P = synth.random_problem(7, 5, 3, 1)
+    c = orc.pyramid(P.D)
+    assert c.shape == (3, 3, 4)
+    ref = np.zeros((3, 3, 4), np.float32)
+    for y in range(5):
+        for x in range(7):
+            ref[:, y // 2, x // 2] += P.D[:, y, x]
+    assert np.array_equal(c, ref)
+
+
+def test_energy_fp64_close_to_reference_type(orc):
+    P = synth.random_problem(40, 30, 16, 9)
+    lab, _ = orc.hbp(P.D, P.V, P.model, 1, 10)
+    e32 = orc.energy(P.D, P.V, lab, exact_type=True)
+    e64 = orc.energy(P.D, P.V, lab)
+    assert abs(e32 - e64) / abs(e64) < 1e-5
+
+
+def test_fp64_standard_oracle_equals_reference_on_linear(orc):
+    """For truncated-linear smoothness the standard rule is the reference rule,
+    so the FP64 oracle lands on the same labels (up to FP32 rounding ties)."""
+    P = synth.random_problem(48, 36, 16, 12)
+    l32, _ = orc.hbp(P.D, P.V, P.model, 1, 20)
+    l64, _ = orc.hbp_f64_std(P.D, P.V, P.model, 1, 20)
+    assert (l32 == l64).mean() > 0.99
