@@ -44,11 +44,11 @@ METRIC = "node-label-iters/s (LBP)"
 UNIT = "node*label*iter/s"
 
 
-def make_problem(kind, seed_offset=0):
+def make_problem(kind, cfg, seed_offset=0):
     from gridinfcuda_gb300 import synth
     if kind == "hbp":
-        return synth.workload_hbp(seed=1 + seed_offset)
-    return synth.workload_plain_bp(seed=0 + seed_offset)
+        return synth.workload_hbp(seed=1 + seed_offset, W=cfg["W"], H=cfg["H"])
+    return synth.workload_plain_bp(seed=0 + seed_offset, W=cfg["W"], H=cfg["H"])
 
 
 def nli_per_step(cfg):
@@ -209,7 +209,7 @@ def run_ours(args, cfg):
     rank, local, world = dist_setup(True)
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    P = make_problem(args.workload, seed_offset=rank)
+    P = make_problem(args.workload, cfg, seed_offset=rank)
     D = torch.from_numpy(P.D).to(dev)
     V = torch.from_numpy(P.V).to(dev)
     lab = torch.zeros((cfg["H"], cfg["W"]), dtype=torch.int32, device=dev)
@@ -293,7 +293,8 @@ def run_ours(args, cfg):
                            "levels": cfg["levels"], "iters_per_level": cfg["iters"], "icm_sweeps": cfg["icm"],
                            "smoothness": "min(|a-b|, 4)" if args.workload == "hbp" else "min(|a-b|, 1.7)",
                            "node_label_iters_per_step": nli, "parallelism": f"replicas x{world}",
-                           "l2": "inputs larger than L2 (costs 531 MB, records 2.8 GB at 1920x1080x64)"},
+                           "l2": f"inputs larger than L2 (costs {W * H * L * 4 / 1e6:.0f} MB, "
+                                 f"records {W * H * L * 20 * 4 / 3 / 1e9:.2f} GB)"},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clock_info,
                 "gpu_launches": int(launches), "energy": energy,
                 "phases_ms": {k: round(stats[-1][k], 4) for k in ("upload_ms", "prepare_ms", "sweep_ms",
@@ -315,7 +316,7 @@ def run_reference(args, cfg):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     import oracle
     oracle.build()
-    P = make_problem(args.workload)
+    P = make_problem(args.workload, cfg)
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
         cpu_port_step(P, cfg, threads)
@@ -349,10 +350,14 @@ def main():
     ap.add_argument("--tile-nodes", type=int, default=0)
     ap.add_argument("--stages", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--size", default=None, help="WxH override of the workload's grid size (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         print("note: the timing rules ask for at least 3 warm-up steps", file=sys.stderr)
-    cfg = WORKLOADS[args.workload]
+    cfg = dict(WORKLOADS[args.workload])
+    if args.size:
+        w, h = (int(v) for v in args.size.lower().split("x"))
+        cfg.update(W=w, H=h, name=cfg["name"].replace(f"{cfg['W']}x{cfg['H']}", f"{w}x{h}"))
     if args.impl == "reference":
         run_reference(args, cfg)
     else:

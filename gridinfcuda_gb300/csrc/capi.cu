@@ -550,6 +550,8 @@ ginf_status export_msgs(Call &c, Prepared &P, const ginf_options *o) {
 
 }  // namespace
 
+void ginf_gpu::set_last_error(const char *msg) { g_last_error = msg; }
+
 // ===========================================================================
 // C ABI
 

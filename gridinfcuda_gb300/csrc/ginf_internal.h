@@ -101,6 +101,9 @@ cudaError_t launch_energy(int ctype, const void *costs, size_t node_stride, size
                           int *status, cudaStream_t s);
 int energy_num_partials(int W, int H);
 cudaError_t launch_convert_table(int src_type, int dst_type, const void *src, void *dst, int n, cudaStream_t s);
+// Sets the message ginf_last_error() returns on this host thread.
+void set_last_error(const char *msg);
+
 cudaError_t launch_stereo_costs(int W, int H, int L, const float *left, const float *right, float coef, float cap,
                                 float *costs, cudaStream_t s);
 

@@ -162,6 +162,27 @@ ginf_status ginf_stereo_costs(int32_t width, int32_t height, int32_t num_labels,
                               const float *left, const float *right, float coef, float cap,
                               float *costs, void *stream);
 
+/* Loopy BP (one level, the reference message rule and stale-belief decode)
+ * that allocates no device memory.  It has no counterpart in the reference.
+ * It is meant for callers that cannot call cudaMalloc while they run: a
+ * real-time loop that cannot afford the device-wide synchronisation and
+ * unbounded latency of cudaMalloc / cudaFree, or a plugin whose host
+ * application owns all device memory.  The caller passes device buffers
+ * (grid->memory must be GINF_DEVICE) and device labels, as for
+ * ginf_decode_hbp; the working set (the message records and a status word)
+ * lives in one fixed array of GINF_NOALLOC_SCRATCH_BYTES in the library's
+ * device image, which every GPU that loads the library holds until the
+ * process exits.  Grids needing more than that (about
+ * GINF_NOALLOC_SCRATCH_BYTES / (20 * L) nodes for FP32 / int32) are rejected
+ * with GINF_ERR_INVALID_ARGUMENT.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  All calls share the
+ * array: calls whose work overlaps on the GPU race and must be serialised by
+ * the caller.  The call synchronises `stream` (a cudaStream_t, NULL = legacy
+ * default stream) before it returns. */
+#define GINF_NOALLOC_SCRATCH_BYTES (48u * 1024u * 1024u)
+ginf_status ginf_decode_bp_noalloc(const ginf_grid *grid, int32_t num_iters, int32_t *labels, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
