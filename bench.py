@@ -215,7 +215,7 @@ def run_ours(args, cfg):
     lab = torch.zeros((cfg["H"], cfg["W"]), dtype=torch.int32, device=dev)
     ws = capi.Workspace()
     stream = torch.cuda.current_stream(dev)
-    opt = dict(stream=stream.cuda_stream, tile_nodes=args.tile_nodes, stages=args.stages)
+    opt = dict(stream=stream.cuda_stream, tile_nodes=args.tile_nodes)
 
     def step():
         return capi.solve(D, V, P.model, cfg["levels"], cfg["iters"], cfg["icm"], labels=lab, workspace=ws,
@@ -348,7 +348,6 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="hbp")
     ap.add_argument("--tile-nodes", type=int, default=0)
-    ap.add_argument("--stages", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", default=None, help="WxH override of the workload's grid size (profiling runs)")
     args = ap.parse_args()

@@ -38,7 +38,7 @@ class Grid(ctypes.Structure):
 
 class Options(ctypes.Structure):
     _fields_ = [("msg_rule", _i32), ("msg_store", _i32), ("decode", _i32), ("normalize", _i32),
-                ("compute_type", _i32), ("tile_nodes", _i32), ("stages", _i32), ("reserved0", _i32),
+                ("compute_type", _i32), ("tile_nodes", _i32), ("reserved1", _i32), ("reserved0", _i32),
                 ("stream", _p), ("msgs_out", _p), ("reserved", ctypes.c_int64 * 6)]
 
 
@@ -159,11 +159,11 @@ def make_grid(D, V, model):
 
 
 def options(rule=RULE_REFERENCE, store=STORE_NATIVE, decode=DECODE_STALE, normalize=NORM_MEAN, compute_type=-1,
-            tile_nodes=0, stages=0, stream=None, msgs_out=None):
+            tile_nodes=0, stream=None, msgs_out=None):
     o = Options()
     lib().ginf_default_options(ctypes.byref(o))
     o.msg_rule, o.msg_store, o.decode, o.normalize = rule, store, decode, normalize
-    o.compute_type, o.tile_nodes, o.stages = compute_type, tile_nodes, stages
+    o.compute_type, o.tile_nodes = compute_type, tile_nodes
     o.stream = stream if stream is not None else None
     o.msgs_out = msgs_out
     return o

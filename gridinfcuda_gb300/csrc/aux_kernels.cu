@@ -26,6 +26,17 @@ __device__ __forceinline__ double msg_to_double<__half>(__half v) {
     return (double)__half2float(v);
 }
 
+// 16-byte loads of E = 16/sizeof(T) consecutive elements.
+template <typename T>
+struct IcmIO {
+    __device__ static void load(const T *p, T *o) {
+        const uint4 v = *reinterpret_cast<const uint4 *>(p);
+        const T *e = reinterpret_cast<const T *>(&v);
+#pragma unroll
+        for (int k = 0; k < (int)(16 / sizeof(T)); ++k) o[k] = e[k];
+    }
+};
+
 constexpr int kThreads = 256;
 
 inline unsigned blocks_for(size_t n, int per_block = kThreads) { return (unsigned)((n + per_block - 1) / per_block); }
@@ -172,36 +183,49 @@ __global__ void k_export(const unsigned char *__restrict__ rec, int W, int H, in
     dst[idx] = v;
 }
 
-// One ICM node update, grid.cc:127-136 and icm.cc:10-34: one warp per node,
-// lane l handles labels l, l+32, ...; cost = D + V(l,f_S) + V(l,f_E) +
-// V(l,f_N) + V(l,f_W) in that order; argmin with the lowest label on ties.
+// One ICM node update, grid.cc:127-136 and icm.cc:10-34: eight lanes per
+// node, lane g taking the 16-byte label chunks g, g+8, ...; the cost of label
+// l is D + V(l,f_S) + V(l,f_E) + V(l,f_N) + V(l,f_W) in that order, with V
+// staged in shared memory row by row (Vs[f*Lp + l] = V(l, f)).  The eight
+// partial first-minima are combined by (value, label), which reproduces the
+// sequential argmin with strict < (lowest label on ties).
 template <typename T>
-__device__ __forceinline__ int icm_node(const unsigned char *rec, int W, int H, int L, uint32_t rec_bytes,
-                                        const T *__restrict__ V, const int32_t *lab, int x, int y, int *status) {
-    const int lane = threadIdx.x & 31;
+__device__ __forceinline__ int icm_node(const unsigned char *rec, int W, int L, int Lp, uint32_t rec_bytes,
+                                        const T *Vs, const int32_t *lab, int x, int y, int g, int *status) {
+    constexpr int E = 16 / sizeof(T);
     const T *D = reinterpret_cast<const T *>(rec + ((size_t)y * W + x) * rec_bytes);
     int f[4];
+#pragma unroll
     for (int d = 0; d < 4; ++d) {
         f[d] = lab[(size_t)(y + ddy(d)) * W + (x + ddx(d))];
         if (f[d] < 0 || f[d] >= L) {
-            if (status && lane == 0) atomicOr(status, DEV_ERR_BOUNDS);
+            if (status && g == 0) atomicOr(status, DEV_ERR_BOUNDS);
             f[d] = 0;
         }
     }
     T best = T(0);
     int bl = 0x7fffffff;
-    for (int l = lane; l < L; l += 32) {
-        T c = D[l];
-        c += V[l + (size_t)L * f[0]];
-        c += V[l + (size_t)L * f[1]];
-        c += V[l + (size_t)L * f[2]];
-        c += V[l + (size_t)L * f[3]];
-        if (bl == 0x7fffffff || c < best) {
-            best = c;
-            bl = l;
+    for (int c = g * E; c < L; c += 8 * E) {
+        T dv[E], v[4][E];
+        IcmIO<T>::load(D + c, dv);
+#pragma unroll
+        for (int d = 0; d < 4; ++d) IcmIO<T>::load(Vs + (size_t)f[d] * Lp + c, v[d]);
+#pragma unroll
+        for (int k = 0; k < E; ++k) {
+            const int i = c + k;
+            T cost = dv[k];
+            cost += v[0][k];
+            cost += v[1][k];
+            cost += v[2][k];
+            cost += v[3][k];
+            if (i < L && (bl == 0x7fffffff || cost < best)) {
+                best = cost;
+                bl = i;
+            }
         }
     }
-    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+    for (int off = 1; off < 8; off <<= 1) {
         const T ob = __shfl_xor_sync(0xffffffffu, best, off);
         const int ol = __shfl_xor_sync(0xffffffffu, bl, off);
         if (ol != 0x7fffffff && (bl == 0x7fffffff || ob < best || (!(best < ob) && ol < bl))) {
@@ -212,16 +236,35 @@ __device__ __forceinline__ int icm_node(const unsigned char *rec, int W, int H, 
     return bl;
 }
 
+// V (L x L, V(l,f) at l + L*f) into shared memory with row stride Lp.
 template <typename T>
-__global__ void k_icm_sync(const unsigned char *__restrict__ rec, int W, int H, int L, uint32_t rec_bytes,
+__device__ __forceinline__ void stage_table(const T *__restrict__ V, T *Vs, int L, int Lp) {
+    for (int i = threadIdx.x; i < L * Lp; i += blockDim.x) {
+        const int f = i / Lp, l = i - f * Lp;
+        Vs[i] = l < L ? V[l + (size_t)L * f] : T(0);
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__global__ void k_icm_sync(const unsigned char *__restrict__ rec, int W, int H, int L, int Lp, uint32_t rec_bytes,
                            const T *__restrict__ V, const int32_t *__restrict__ old_lab, int32_t *__restrict__ new_lab,
                            int *status) {
-    const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    extern __shared__ __align__(16) unsigned char icm_smem[];
+    T *Vs = reinterpret_cast<T *>(icm_smem);
+    stage_table(V, Vs, L, Lp);
     const size_t n = (size_t)(W - 2) * (H - 2);
-    if (warp >= n) return;
-    const int x = 1 + (int)(warp % (W - 2)), y = 1 + (int)(warp / (W - 2));
-    const int bl = icm_node<T>(rec, W, H, L, rec_bytes, V, old_lab, x, y, status);
-    if ((threadIdx.x & 31) == 0) new_lab[(size_t)y * W + x] = bl;
+    const int g = threadIdx.x & 7;
+    // Node groups are whole 8-lane slices of a warp, so every group either
+    // has a node or the whole slice skips it together.
+    for (size_t base = (size_t)blockIdx.x * (blockDim.x / 8); base < n; base += (size_t)gridDim.x * (blockDim.x / 8)) {
+        const size_t node = base + (threadIdx.x >> 3);
+        const bool act = node < n;
+        const size_t nn = act ? node : 0;
+        const int x = 1 + (int)(nn % (W - 2)), y = 1 + (int)(nn / (W - 2));
+        const int bl = icm_node<T>(rec, W, L, Lp, rec_bytes, Vs, old_lab, x, y, g, status);
+        if (act && g == 0) new_lab[(size_t)y * W + x] = bl;
+    }
 }
 
 // Raster Gauss-Seidel (icm.cc:40-67) as an exact wavefront: on anti-diagonal
@@ -229,15 +272,17 @@ __global__ void k_icm_sync(const unsigned char *__restrict__ rec, int W, int H, 
 // updated and its east and south neighbours (s+1) are not, exactly as in the
 // raster order, and nodes of one diagonal are never adjacent.
 template <typename T>
-__global__ void k_icm_diag(const unsigned char *__restrict__ rec, int W, int H, int L, uint32_t rec_bytes,
+__global__ void k_icm_diag(const unsigned char *__restrict__ rec, int W, int H, int L, int Lp, uint32_t rec_bytes,
                            const T *__restrict__ V, int32_t *lab, int s, int *status) {
-    const int warp = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    extern __shared__ __align__(16) unsigned char icm_smem[];
+    T *Vs = reinterpret_cast<T *>(icm_smem);
+    stage_table(V, Vs, L, Lp);
     const int ylo = max(1, s - (W - 2)), yhi = min(H - 2, s - 1);
-    const int y = ylo + warp;
-    if (y > yhi) return;
-    const int x = s - y;
-    const int bl = icm_node<T>(rec, W, H, L, rec_bytes, V, lab, x, y, status);
-    if ((threadIdx.x & 31) == 0) lab[(size_t)y * W + x] = bl;
+    const int idx = blockIdx.x * (blockDim.x / 8) + (threadIdx.x >> 3);
+    const bool act = ylo + idx <= yhi;
+    const int y = act ? ylo + idx : ylo, x = s - y;
+    const int bl = icm_node<T>(rec, W, L, Lp, rec_bytes, Vs, lab, x, y, threadIdx.x & 7, status);
+    if (act && (threadIdx.x & 7) == 0) lab[(size_t)y * W + x] = bl;
 }
 
 // Energy, grid.cc:102-125, in FP64: block partial sums over a fixed
@@ -398,12 +443,46 @@ cudaError_t launch_export_messages(const RecordFormat &f, const unsigned char *r
     return cudaGetLastError();
 }
 
+// Shared memory for the staged table, raising the kernel's limit once when
+// it exceeds the default 48 KB.
+template <typename K>
+cudaError_t icm_smem_attr(K kern, size_t bytes) {
+    static size_t configured = 48 * 1024;
+    if (bytes > configured) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (e != cudaSuccess) return e;
+        configured = bytes;
+    }
+    return cudaSuccess;
+}
+
+int g_num_sms = 0;
+
+int num_sms() {
+    if (g_num_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_num_sms <= 0) g_num_sms = 1;
+    }
+    return g_num_sms;
+}
+
 cudaError_t launch_icm_sync(const RecordFormat &f, const unsigned char *rec, int W, int H, const void *V,
                             const int32_t *old_labels, int32_t *new_labels, int *status, cudaStream_t s) {
     if (W < 3 || H < 3) return cudaSuccess;
     const size_t n = (size_t)(W - 2) * (H - 2);
-    GINF_DISPATCH_T(f, { k_icm_sync<T><<<blocks_for(n * 32), kThreads, 0, s>>>(
-                             rec, W, H, f.L, f.rec_bytes, static_cast<const T *>(V), old_labels, new_labels, status); })
+    GINF_DISPATCH_T(f, {
+        const size_t smem = (size_t)f.L * f.Lp * sizeof(T);
+        cudaError_t e = icm_smem_attr(k_icm_sync<T>, smem);
+        if (e != cudaSuccess) return e;
+        size_t blocks = (n + kThreads / 8 - 1) / (kThreads / 8);
+        const size_t cap = (size_t)num_sms() * 8;
+        if (blocks > cap) blocks = cap;
+        k_icm_sync<T><<<(unsigned)blocks, kThreads, smem, s>>>(rec, W, H, f.L, f.Lp, f.rec_bytes,
+                                                               static_cast<const T *>(V), old_labels, new_labels,
+                                                               status);
+    })
     return cudaGetLastError();
 }
 
@@ -413,9 +492,13 @@ cudaError_t launch_icm_async_diag(const RecordFormat &f, const unsigned char *re
     const int yhi = diag - 1 < H - 2 ? diag - 1 : H - 2;
     if (yhi < ylo) return cudaSuccess;
     const size_t n = (size_t)(yhi - ylo + 1);
-    GINF_DISPATCH_T(f, { k_icm_diag<T><<<blocks_for(n * 32), kThreads, 0, s>>>(rec, W, H, f.L, f.rec_bytes,
-                                                                             static_cast<const T *>(V), labels, diag,
-                                                                             status); })
+    GINF_DISPATCH_T(f, {
+        const size_t smem = (size_t)f.L * f.Lp * sizeof(T);
+        cudaError_t e = icm_smem_attr(k_icm_diag<T>, smem);
+        if (e != cudaSuccess) return e;
+        k_icm_diag<T><<<blocks_for(n * 8), kThreads, smem, s>>>(rec, W, H, f.L, f.Lp, f.rec_bytes,
+                                                                static_cast<const T *>(V), labels, diag, status);
+    })
     return cudaGetLastError();
 }
 

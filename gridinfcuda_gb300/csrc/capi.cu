@@ -216,11 +216,9 @@ ginf_status resolve(const ginf_grid *g, const ginf_options *o, Resolved &r) {
     else r.mode = MODE_STD_MINCONV;
     r.norm_min = (o->normalize == GINF_NORM_MIN || r.store == ST_F16) ? 1 : 0;
     r.decode = o->decode;
-    r.cfg.nt = o->tile_nodes == 64 ? 64 : 32;
-    r.cfg.stages = o->stages == 2 ? 2 : 1;
-    if (o->tile_nodes != 0 && o->tile_nodes != 32 && o->tile_nodes != 64)
-        return fail(GINF_ERR_INVALID_ARGUMENT, "tile_nodes must be 0, 32 or 64");
-    if (o->stages < 0 || o->stages > 2) return fail(GINF_ERR_INVALID_ARGUMENT, "stages must be 0, 1 or 2");
+    if (o->tile_nodes != 0 && o->tile_nodes != 8 && o->tile_nodes != 16 && o->tile_nodes != 32)
+        return fail(GINF_ERR_INVALID_ARGUMENT, "tile_nodes must be 0, 8, 16 or 32");
+    r.cfg.nt = o->tile_nodes == 0 ? 16 : o->tile_nodes;
     r.stream = static_cast<cudaStream_t>(o->stream);
     return GINF_OK;
 }

@@ -61,13 +61,13 @@ struct SweepParams {
                                    // V(0,L-1) from it, as bp.cc:35,43 do
     int32_t *labels;               // level-0 labels (W*H) or nullptr
     int write_labels;
-    int tiles_per_row, num_tiles;
+    int tiles_per_row, num_tiles;  // set by the launcher for the variant it runs
     int *status;
 };
 
+// Nodes per sweep tile (8, 16 or 32; 16 unless a tuned choice says otherwise).
 struct SweepConfig {
-    int nt = 32;       // nodes (threads) per tile
-    int stages = 1;    // shared-memory pipeline depth
+    int nt = 16;
 };
 
 // Launch one half-sweep; returns the kernel launch error.

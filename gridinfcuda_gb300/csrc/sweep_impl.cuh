@@ -1,21 +1,10 @@
 // sweep_impl.cuh -- the checkerboard half-sweep kernel (one BP "iteration").
 //
-// Work split: one thread per updated node, NT same-colour nodes of one grid
-// row per tile.  Per tile:
-//   1. every thread issues one bulk TMA copy of its node's record (costs plus
-//      the four incoming messages, rec_bytes contiguous bytes) into its own
-//      padded shared-memory slot; completion is counted in bytes on the
-//      stage's mbarrier (the slot stride is an odd number of 16-byte chunks,
-//      so the 128-bit shared loads below are free of bank conflicts);
-//   2. the thread forms the belief from = D + m_S + m_E + m_N + m_W, its
-//      argmin (the reference's stale-belief label, bp.cc:65-84), and the four
-//      outgoing messages, each written over the incoming slot it replaces;
-//   3. four bulk TMA stores move the outgoing messages into the neighbours'
-//      records (stored at the receiver, slot OPP(d)).
-// With STAGES == 2 the next tile's copies are in flight while the current one
-// is computed.  The sequential per-thread update reproduces the reference's
-// operation order exactly (src/bp.cc:7-63), so f32 and i32 results are
-// bit-identical to the CPU code.
+// Each message is computed by one thread with the reference's operation
+// order (src/bp.cc:7-63): sequential min-plus scans, (a<b)?a:b minima, the
+// mean by IEEE division.  FP32 and int32 results are therefore bit-identical
+// to the reference's CPU code.  The kernel itself is described above
+// sweep_kernel at the end of this file.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -155,132 +144,138 @@ __device__ __forceinline__ unsigned zero_mask(const SweepParams &p, int x, int y
     return z;
 }
 
-// from = D + in_S + in_E + in_N + in_W per label, in the order of bp.cc:10-17,
-// plus its first argmin (strict <, bp.cc:74-80).  The belief goes to fr[]
-// (registers) when FR_REGS, else over the D region of the slot.
-template <typename T, typename M, int LMAX, bool FR_REGS>
-__device__ __forceinline__ void collect(const SweepParams &p, unsigned char *slot, unsigned zmask, T *fr, int &label) {
+__device__ __forceinline__ void zero_bytes(unsigned char *p, uint32_t bytes) {
+    for (uint32_t o = 0; o < bytes; o += 16) *reinterpret_cast<uint4 *>(p + o) = make_uint4(0, 0, 0, 0);
+}
+
+// val / L in T arithmetic.  With L a compile-time power of two the division is
+// a multiplication by the exact reciprocal, which rounds identically.
+template <typename T, int LMAX, bool EXACT>
+__device__ __forceinline__ T mean_of(T sum, int L) {
+    if constexpr (EXACT && (LMAX & (LMAX - 1)) == 0 && !std::is_same<T, int>::value) {
+        return sum * (T(1) / T(LMAX));
+    } else if constexpr (EXACT) {
+        return div_labels(sum, LMAX);
+    } else {
+        return div_labels(sum, L);
+    }
+}
+
+// Belief of one node, computed by its four lanes together: lane `dir` takes
+// the 16-byte message chunks dir, dir+4, dir+8, ...  For each label,
+// from = D + in_S + in_E + in_N + in_W in that order (bp.cc:10-17); the sum
+// overwrites D in shared memory.  Returns the lane's first minimum (value,
+// label); labels are visited in increasing order, so combining the four
+// partial results by (value, label) gives the reference's first argmin
+// (strict <, bp.cc:74-80).
+template <typename T, typename M, int LMAX, bool EXACT>
+__device__ __forceinline__ void belief_part(const SweepParams &p, unsigned char *slot, int L, int dir, T &best,
+                                            int &bl) {
     constexpr int B = MIO<M, T>::B;
-    const int L = p.L;
-    unsigned char *mb = slot + p.d_bytes;
-    T best = T(0);
-    int bl = 0;
+    constexpr int NCH = (LMAX + B - 1) / B;
+    const unsigned char *mb = slot + p.d_bytes;
 #pragma unroll
-    for (int c = 0; c < LMAX; c += B) {
-        if (c < L) {
+    for (int j = 0; j < (NCH + 3) / 4; ++j) {
+        const int c = (4 * j + dir) * B;
+        if (c < LMAX && (EXACT || c < L)) {
             T v[B], a[B];
             load_t<T, B>(slot + c * sizeof(T), v);
 #pragma unroll
-            for (int d = 0; d < 4; ++d) {
-                MIO<M, T>::load(mb + d * p.m_bytes + c * sizeof(M), a);
-                const bool z = (zmask >> d) & 1u;
+            for (int e = 0; e < 4; ++e) {
+                MIO<M, T>::load(mb + e * p.m_bytes + c * sizeof(M), a);
 #pragma unroll
-                for (int k = 0; k < B; ++k) v[k] = v[k] + (z ? T(0) : a[k]);
+                for (int kk = 0; kk < B; ++kk) v[kk] = v[kk] + a[kk];
             }
+            store_t<T, B>(slot + c * sizeof(T), v);
 #pragma unroll
-            for (int k = 0; k < B; ++k) {
-                const int i = c + k;
-                if (i == 0) {
-                    best = v[k];
-                    bl = 0;
-                } else if (i < L && v[k] < best) {
-                    best = v[k];
+            for (int kk = 0; kk < B; ++kk) {
+                const int i = c + kk;
+                if ((EXACT || i < L) && (bl == 0x7fffffff || v[kk] < best)) {
+                    best = v[kk];
                     bl = i;
                 }
             }
-            if constexpr (FR_REGS) {
-#pragma unroll
-                for (int k = 0; k < B; ++k) fr[c + k] = v[k];
-            } else {
-                store_t<T, B>(slot + c * sizeof(T), v);
-            }
         }
     }
-    label = bl;
 }
 
-// Truncated-linear / Potts messages (bp.cc:26-54), all four directions.
-template <typename T, typename M, int LMAX, bool FR_REGS>
-__device__ __forceinline__ void messages_linear(const SweepParams &p, unsigned char *slot, unsigned zmask, const T *fr) {
-    constexpr int B = MIO<M, T>::B;
-    const int L = p.L;
-    const T *Vt = static_cast<const T *>(p.V);
-    const T scale = __ldg(&Vt[L]), trunc = __ldg(&Vt[(size_t)L * (L - 1)]);  // V(0,1), V(0,L-1): bp.cc:35,43
-    unsigned char *mb = slot + p.d_bytes;
-#pragma unroll 1
-    for (int d = 0; d < 4; ++d) {
-        const bool zd = (zmask >> d) & 1u;
-        unsigned char *md = mb + d * p.m_bytes;
-        T o[LMAX];
+// Combines (value, label) partial minima of the four lanes of a node
+// (lanes k, k+8, k+16, k+24): smaller value wins, equal values go to the
+// lower label; 0x7fffffff marks an empty partial.
+template <typename T>
+__device__ __forceinline__ void argmin_combine(T &best, int &bl) {
 #pragma unroll
-        for (int c = 0; c < LMAX; c += B) {
-            if (c < L) {
-                T a[B], f[B];
-                MIO<M, T>::load(md + c * sizeof(M), a);
-                if constexpr (FR_REGS) {
-#pragma unroll
-                    for (int k = 0; k < B; ++k) f[k] = fr[c + k];
-                } else {
-                    load_t<T, B>(slot + c * sizeof(T), f);
-                }
-#pragma unroll
-                for (int k = 0; k < B; ++k) o[c + k] = f[k] - (zd ? T(0) : a[k]);
-            }
+    for (int off = 8; off <= 16; off <<= 1) {
+        const T ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int ol = __shfl_xor_sync(0xffffffffu, bl, off);
+        const bool take = ol != 0x7fffffff && (bl == 0x7fffffff || ob < best || (!(best < ob) && ol < bl));
+        if (take) {
+            best = ob;
+            bl = ol;
         }
-        T minh = o[0];
+    }
+}
+
+// Truncated-linear / Potts message towards `dir` (bp.cc:26-54), one lane:
+// h = from - in[dir], min of h, forward and backward min-plus scans with slope
+// V(0,1), truncation at min(h) + V(0,L-1), subtraction of the mean (or the
+// minimum), written over in[dir].
+template <typename T, typename M, int LMAX, bool EXACT>
+__device__ __forceinline__ void message_linear(const SweepParams &p, unsigned char *slot, int L, int dir, T scale,
+                                               T trunc) {
+    constexpr int B = MIO<M, T>::B;
+    unsigned char *md = slot + p.d_bytes + dir * p.m_bytes;
+    T o[LMAX];
+#pragma unroll
+    for (int c = 0; c < LMAX; c += B) {
+        if (EXACT || c < L) {
+            T a[B], f[B];
+            MIO<M, T>::load(md + c * sizeof(M), a);
+            load_t<T, B>(slot + c * sizeof(T), f);
+#pragma unroll
+            for (int k = 0; k < B; ++k) o[c + k] = f[k] - a[k];
+        }
+    }
+    T minh = o[0];
+#pragma unroll
+    for (int i = 1; i < LMAX; ++i)
+        if (EXACT || i < L) minh = rmin(minh, o[i]);
+#pragma unroll
+    for (int i = 1; i < LMAX; ++i)
+        if (EXACT || i < L) o[i] = rmin(o[i], o[i - 1] + scale);
+#pragma unroll
+    for (int i = LMAX - 2; i >= 0; --i)
+        if (EXACT || i + 1 < L) o[i] = rmin(o[i], o[i + 1] + scale);
+    minh += trunc;
+    T val = T(0);
+#pragma unroll
+    for (int i = 0; i < LMAX; ++i)
+        if (EXACT || i < L) {
+            o[i] = rmin(o[i], minh);
+            val += o[i];
+        }
+    if (p.norm_min) {
+        val = o[0];
 #pragma unroll
         for (int i = 1; i < LMAX; ++i)
-            if (i < L) minh = rmin(minh, o[i]);
+            if (EXACT || i < L) val = rmin(val, o[i]);
+    } else {
+        val = mean_of<T, LMAX, EXACT>(val, L);
+    }
 #pragma unroll
-        for (int i = 1; i < LMAX; ++i)
-            if (i < L) o[i] = rmin(o[i], o[i - 1] + scale);
+    for (int c = 0; c < LMAX; c += B) {
+        if (EXACT || c < L) {
+            T r[B];
 #pragma unroll
-        for (int i = LMAX - 2; i >= 0; --i)
-            if (i + 1 < L) o[i] = rmin(o[i], o[i + 1] + scale);
-        minh += trunc;
-        T val = T(0);
-#pragma unroll
-        for (int i = 0; i < LMAX; ++i)
-            if (i < L) {
-                o[i] = rmin(o[i], minh);
-                val += o[i];
-            }
-        if (p.norm_min) {
-            val = o[0];
-#pragma unroll
-            for (int i = 1; i < LMAX; ++i)
-                if (i < L) val = rmin(val, o[i]);
-        } else {
-            val = div_labels(val, L);
-        }
-#pragma unroll
-        for (int c = 0; c < LMAX; c += B) {
-            if (c < L) {
-                T r[B];
-#pragma unroll
-                for (int k = 0; k < B; ++k) r[k] = o[c + k] - val;
-                MIO<M, T>::store(md + c * sizeof(M), r);
-            }
+            for (int k = 0; k < B; ++k) r[k] = o[c + k] - val;
+            MIO<M, T>::store(md + c * sizeof(M), r);
         }
     }
 }
 
-// Writes o[0..L) (then padding up to the chunk boundary) into message slot md.
+// h = from - in[dir] into local h[] (from is over the D region of the slot).
 template <typename T, typename M, int LMAX>
-__device__ __forceinline__ void store_msg(unsigned char *md, const T *o, int L) {
-    constexpr int B = MIO<M, T>::B;
-#pragma unroll 1
-    for (int c = 0; c < L; c += B) {
-        T r[B];
-#pragma unroll
-        for (int k = 0; k < B; ++k) r[k] = (c + k < L) ? o[c + k] : T(0);
-        MIO<M, T>::store(md + c * sizeof(M), r);
-    }
-}
-
-// h = from - incoming (from over the D region of the slot), into local h[].
-template <typename T, typename M, int LMAX>
-__device__ __forceinline__ void load_h(const unsigned char *slot, const unsigned char *md, bool zd, int L, T *h) {
+__device__ __forceinline__ void load_h(const unsigned char *slot, const unsigned char *md, int L, T *h) {
     constexpr int B = MIO<M, T>::B;
 #pragma unroll 1
     for (int c = 0; c < L; c += B) {
@@ -289,7 +284,7 @@ __device__ __forceinline__ void load_h(const unsigned char *slot, const unsigned
         load_t<T, B>(slot + c * sizeof(T), f);
 #pragma unroll
         for (int k = 0; k < B; ++k)
-            if (c + k < LMAX) h[c + k] = f[k] - (zd ? T(0) : a[k]);
+            if (c + k < LMAX) h[c + k] = f[k] - a[k];
     }
 }
 
@@ -307,241 +302,258 @@ __device__ __forceinline__ void normalise(T *o, int L, int norm_min) {
     for (int i = 0; i < L; ++i) o[i] -= val;
 }
 
+// Writes o[0..L) (zero padding to the chunk boundary) into message slot md.
+template <typename T, typename M>
+__device__ __forceinline__ void store_msg(unsigned char *md, const T *o, int L) {
+    constexpr int B = MIO<M, T>::B;
+#pragma unroll 1
+    for (int c = 0; c < L; c += B) {
+        T r[B];
+#pragma unroll
+        for (int k = 0; k < B; ++k) r[k] = (c + k < L) ? o[c + k] : T(0);
+        MIO<M, T>::store(md + c * sizeof(M), r);
+    }
+}
+
 // Reference rule for EXPLICIT / TRUNC_QUAD (bp.cc:55-62): the same vector
 // out(i) = min_j V(i,j) + from(j) goes out in all four directions, without
-// subtracting the receiver's message and without normalisation.
+// subtracting the receiver's message and without normalisation.  Lane `dir`
+// computes the chunks dir, dir+4, ... and writes them into all four slots.
 template <typename T, typename M, int LMAX>
-__device__ void messages_ref_minconv(const SweepParams &p, unsigned char *slot) {
-    const int L = p.L;
+__device__ void messages_ref_minconv(const SweepParams &p, unsigned char *slot, int L, int dir) {
+    constexpr int B = MIO<M, T>::B;
     const T *V = static_cast<const T *>(p.V);
     const T *fr = reinterpret_cast<const T *>(slot);
-    T o[LMAX];
-#pragma unroll 1
-    for (int i = 0; i < L; ++i) {
-        T m = __ldg(&V[i]) + fr[0];
-#pragma unroll 1
-        for (int j = 0; j < L; ++j) m = rmin(m, __ldg(&V[i + (size_t)L * j]) + fr[j]);
-        o[i] = m;
-    }
     unsigned char *mb = slot + p.d_bytes;
 #pragma unroll 1
-    for (int d = 0; d < 4; ++d) store_msg<T, M, LMAX>(mb + d * p.m_bytes, o, L);
+    for (int c = dir * B; c < L; c += 4 * B) {
+        T r[B];
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+            const int i = c + k;
+            T m = T(0);
+            if (i < L) {
+                m = __ldg(&V[i]) + fr[0];
+#pragma unroll 1
+                for (int j = 0; j < L; ++j) m = rmin(m, __ldg(&V[i + (size_t)L * j]) + fr[j]);
+            }
+            r[k] = m;
+        }
+#pragma unroll 1
+        for (int e = 0; e < 4; ++e) MIO<M, T>::store(mb + e * p.m_bytes + c * sizeof(M), r);
+    }
 }
 
 // Standard rule, EXPLICIT model: O(L^2) min-convolution of h = from - in.
 template <typename T, typename M, int LMAX>
-__device__ void messages_std_minconv(const SweepParams &p, unsigned char *slot, unsigned zmask) {
-    const int L = p.L;
+__device__ void message_std_minconv(const SweepParams &p, unsigned char *slot, int L, int dir) {
     const T *V = static_cast<const T *>(p.V);
-    unsigned char *mb = slot + p.d_bytes;
+    unsigned char *md = slot + p.d_bytes + dir * p.m_bytes;
     T h[LMAX], o[LMAX];
+    load_h<T, M, LMAX>(slot, md, L, h);
 #pragma unroll 1
-    for (int d = 0; d < 4; ++d) {
-        unsigned char *md = mb + d * p.m_bytes;
-        load_h<T, M, LMAX>(slot, md, (zmask >> d) & 1u, L, h);
+    for (int i = 0; i < L; ++i) {
+        T m = __ldg(&V[i]) + h[0];
 #pragma unroll 1
-        for (int i = 0; i < L; ++i) {
-            T m = __ldg(&V[i]) + h[0];
-#pragma unroll 1
-            for (int j = 1; j < L; ++j) m = rmin(m, __ldg(&V[i + (size_t)L * j]) + h[j]);
-            o[i] = m;
-        }
-        normalise(o, L, p.norm_min);
-        store_msg<T, M, LMAX>(md, o, L);
+        for (int j = 1; j < L; ++j) m = rmin(m, __ldg(&V[i + (size_t)L * j]) + h[j]);
+        o[i] = m;
     }
+    normalise(o, L, p.norm_min);
+    store_msg<T, M>(md, o, L);
 }
 
 // Standard rule, truncated quadratic: O(L) lower envelope of parabolas
 // (Felzenszwalb & Huttenlocher, "Distance Transforms of Sampled Functions",
 // Theory of Computing 8, 2012), then truncation at min(h) + V(0, L-1).
 template <typename T, typename M, int LMAX>
-__device__ void messages_std_quad(const SweepParams &p, unsigned char *slot, unsigned zmask) {
+__device__ void message_std_quad(const SweepParams &p, unsigned char *slot, int L, int dir, T s, T trunc) {
     if constexpr (std::is_same<T, int>::value) {
         return;  // integer grids use the exact O(L^2) rule instead (host side)
     } else {
-        const int L = p.L;
-        const T *Vt = static_cast<const T *>(p.V);
-        const T s = __ldg(&Vt[L]), trunc = __ldg(&Vt[(size_t)L * (L - 1)]);
-        unsigned char *mb = slot + p.d_bytes;
+        unsigned char *md = slot + p.d_bytes + dir * p.m_bytes;
         T h[LMAX], o[LMAX], z[LMAX + 1];
         int v[LMAX];
+        load_h<T, M, LMAX>(slot, md, L, h);
+        T minh = h[0];
+        for (int i = 1; i < L; ++i) minh = h[i] < minh ? h[i] : minh;
+        if (!(s > T(0))) {
+            for (int i = 0; i < L; ++i) o[i] = minh;
+        } else {
+            int k = 0;
+            v[0] = 0;
+            z[0] = -pos_inf<T>();
+            z[1] = pos_inf<T>();
 #pragma unroll 1
-        for (int d = 0; d < 4; ++d) {
-            unsigned char *md = mb + d * p.m_bytes;
-            load_h<T, M, LMAX>(slot, md, (zmask >> d) & 1u, L, h);
-            T minh = h[0];
-            for (int i = 1; i < L; ++i) minh = h[i] < minh ? h[i] : minh;
-            if (!(s > T(0))) {
-                for (int i = 0; i < L; ++i) o[i] = minh;
-            } else {
-                int k = 0;
-                v[0] = 0;
-                z[0] = -pos_inf<T>();
-                z[1] = pos_inf<T>();
-#pragma unroll 1
-                for (int q = 1; q < L; ++q) {
-                    T sq;
-                    for (;;) {
-                        const int pp = v[k];
-                        sq = ((h[q] + s * T(q) * T(q)) - (h[pp] + s * T(pp) * T(pp))) / (T(2) * s * T(q - pp));
-                        if (sq <= z[k] && k > 0) {
-                            --k;
-                            continue;
-                        }
-                        break;
-                    }
-                    if (sq <= z[k]) {
-                        v[0] = q;
-                        z[0] = -pos_inf<T>();
-                        z[1] = pos_inf<T>();
+            for (int q = 1; q < L; ++q) {
+                T sq;
+                for (;;) {
+                    const int pp = v[k];
+                    sq = ((h[q] + s * T(q) * T(q)) - (h[pp] + s * T(pp) * T(pp))) / (T(2) * s * T(q - pp));
+                    if (sq <= z[k] && k > 0) {
+                        --k;
                         continue;
                     }
-                    ++k;
-                    v[k] = q;
-                    z[k] = sq;
-                    z[k + 1] = pos_inf<T>();
+                    break;
                 }
-                k = 0;
-#pragma unroll 1
-                for (int q = 0; q < L; ++q) {
-                    while (z[k + 1] < T(q)) ++k;
-                    const int pp = v[k];
-                    o[q] = s * T(q - pp) * T(q - pp) + h[pp];
+                if (sq <= z[k]) {
+                    v[0] = q;
+                    z[0] = -pos_inf<T>();
+                    z[1] = pos_inf<T>();
+                    continue;
                 }
+                ++k;
+                v[k] = q;
+                z[k] = sq;
+                z[k + 1] = pos_inf<T>();
             }
-            const T cap = minh + trunc;
-            for (int i = 0; i < L; ++i) o[i] = rmin(o[i], cap);
-            normalise(o, L, p.norm_min);
-            store_msg<T, M, LMAX>(md, o, L);
+            k = 0;
+#pragma unroll 1
+            for (int q = 0; q < L; ++q) {
+                while (z[k + 1] < T(q)) ++k;
+                const int pp = v[k];
+                o[q] = s * T(q - pp) * T(q - pp) + h[pp];
+            }
         }
+        const T cap = minh + trunc;
+        for (int i = 0; i < L; ++i) o[i] = rmin(o[i], cap);
+        normalise(o, L, p.norm_min);
+        store_msg<T, M>(md, o, L);
     }
 }
 
-// LINEAR_ONLY instantiations carry only the truncated-linear / Potts update
-// (the hot path), so their register allocation is not shaped by the
-// local-memory arrays of the O(L^2) and lower-envelope rules.
-template <typename T, typename M, int LMAX, int NT, int STAGES, bool LINEAR_ONLY>
-__global__ void __launch_bounds__(NT) sweep_kernel(const SweepParams p) {
+// One checkerboard half-sweep.  Block = NW warps, tile = 8*NW consecutive
+// same-colour nodes of one row; lane = (node k = lane & 7, direction
+// dir = lane >> 3).  Per tile:
+//   1. lane (k, 0) brings the node's whole record into the node's padded
+//      shared-memory slot with one bulk TMA copy (complete_tx on the
+//      block's mbarrier; the first sweep of a level fetches D and, per lane,
+//      one incoming slot from the coarser level instead);
+//   2. incoming slots whose sender is a border node are zeroed;
+//   3. the node's four lanes form the belief over D and its first argmin;
+//   4. lane (k, dir) forms the message towards dir over its incoming slot;
+//   5. lane (k, dir) bulk-stores it into the neighbour's record, slot
+//      OPP(dir).
+// Lanes 0-7 of a warp are eight different nodes with the same direction; the
+// odd slot stride in 16-byte chunks puts their 128-bit shared accesses in
+// eight different bank groups.
+template <typename T, typename M, int LMAX, bool EXACT, int NW, bool LINEAR_ONLY>
+__global__ void __launch_bounds__(NW * 32) sweep_kernel(const SweepParams p) {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ uint64_t full_bar[STAGES];
-    constexpr bool FR_REGS = LMAX * sizeof(T) <= 256;
-    const int tid = threadIdx.x;
+    __shared__ uint64_t full_bar;
+    constexpr int NN = NW * 8;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int dir = lane >> 3;
+    const int node = (tid >> 5) * 8 + (lane & 7);
+    const int L = EXACT ? LMAX : p.L;
+    unsigned char *slot = smem + (size_t)node * p.slot_bytes;
+    const T *Vt = static_cast<const T *>(p.V);
+    const T scale = __ldg(&Vt[L]), trunc = __ldg(&Vt[(size_t)L * (L - 1)]);  // V(0,1), V(0,L-1): bp.cc:35,43
     if (tid == 0) {
-#pragma unroll
-        for (int s = 0; s < STAGES; ++s) mbar_init(&full_bar[s], NT);
+        mbar_init(&full_bar, NW * 32);
         fence_barrier_init();
     }
     __syncthreads();
 
-    auto node_of = [&](int t, int &x, int &y) -> bool {
+    auto node_xy = [&](int t, int &x, int &y) -> bool {
         y = 1 + t / p.tiles_per_row;
-        const int k = (t % p.tiles_per_row) * NT + tid;
-        x = ((y + p.iter) & 1) + 1 + 2 * k;
+        const int kk = (t % p.tiles_per_row) * NN + node;
+        x = ((y + p.iter) & 1) + 1 + 2 * kk;
         return x <= p.W - 2;
     };
 
-    auto issue_load = [&](int t, int s) {
+    auto issue_load = [&](int t) {
         int x, y;
-        const bool act = node_of(t, x, y);
-        unsigned char *slot = smem + (size_t)(s * NT + tid) * p.slot_bytes;
-        const unsigned char *r = p.rec + ((size_t)y * p.W + x) * p.rec_bytes;
+        const bool act = node_xy(t, x, y);
         uint32_t bytes = 0;
-        unsigned want = 0;  // coarse slots to fetch (RD_COARSE)
+        bool want = false;
         if (act) {
             if (p.read_mode == RD_OWN) {
-                bytes = p.rec_bytes;
+                if (dir == 0) bytes = p.rec_bytes;
             } else {
-                bytes = p.d_bytes;
+                if (dir == 0) bytes = p.d_bytes;
                 if (p.read_mode == RD_COARSE) {
-                    want = ~zero_mask(p, x, y) & 0xFu;
-                    bytes += __popc(want) * p.m_bytes;
+                    want = !((zero_mask(p, x, y) >> dir) & 1u);
+                    if (want) bytes += p.m_bytes;
                 }
             }
         }
-        mbar_arrive_expect_tx(&full_bar[s], bytes);
+        mbar_arrive_expect_tx(&full_bar, bytes);
         if (act) {
+            const unsigned char *r = p.rec + ((size_t)y * p.W + x) * p.rec_bytes;
             if (p.read_mode == RD_OWN) {
-                bulk_load(slot, r, p.rec_bytes, &full_bar[s]);
+                if (dir == 0) bulk_load(slot, r, p.rec_bytes, &full_bar);
             } else {
-                bulk_load(slot, r, p.d_bytes, &full_bar[s]);
-#pragma unroll
-                for (int d = 0; d < 4; ++d) {
-                    if ((want >> d) & 1u) {
-                        // The coarse node Q = (node + dir(d)) / 2 sent its message
-                        // towards -dir(d); it is stored at R = Q - dir(d), slot d.
-                        const int Qx = (x + dir_dx(d)) >> 1, Qy = (y + dir_dy(d)) >> 1;
-                        const int Rx = Qx - dir_dx(d), Ry = Qy - dir_dy(d);
-                        const unsigned char *src =
-                            p.crec + ((size_t)Ry * p.cW + Rx) * p.rec_bytes + p.d_bytes + d * p.m_bytes;
-                        bulk_load(slot + p.d_bytes + d * p.m_bytes, src, p.m_bytes, &full_bar[s]);
-                    }
+                if (dir == 0) bulk_load(slot, r, p.d_bytes, &full_bar);
+                if (want) {
+                    // The coarse node Q = (node + dir) / 2 sent its message towards
+                    // -dir; it is stored at R = Q - dir, slot dir.
+                    const int Qx = (x + dir_dx(dir)) >> 1, Qy = (y + dir_dy(dir)) >> 1;
+                    const int Rx = Qx - dir_dx(dir), Ry = Qy - dir_dy(dir);
+                    const unsigned char *src =
+                        p.crec + ((size_t)Ry * p.cW + Rx) * p.rec_bytes + p.d_bytes + dir * p.m_bytes;
+                    bulk_load(slot + p.d_bytes + dir * p.m_bytes, src, p.m_bytes, &full_bar);
                 }
             }
         }
     };
 
-    const int first = blockIdx.x;
-#pragma unroll
-    for (int s = 0; s < STAGES; ++s) {
-        const int t = first + s * gridDim.x;
-        if (t < p.num_tiles) issue_load(t, s);
-    }
-
-    bool ok = true;
-    for (int j = 0;; ++j) {
-        const int t = first + j * gridDim.x;
-        if (t >= p.num_tiles) break;
-        const int s = j % STAGES;
-        const uint32_t parity = (uint32_t)(j / STAGES) & 1u;
+    int t = blockIdx.x;
+    if (t < p.num_tiles) issue_load(t);
+    uint32_t parity = 0;
+    for (; t < p.num_tiles; t += gridDim.x) {
         // Every thread's wait is bounded; the vote makes giving up block-uniform
-        // so no thread is left behind at a later __syncthreads.
-        const bool got = mbar_wait_bounded(&full_bar[s], parity, p.status);
-        if (!__syncthreads_and(got)) {
-            ok = false;
-            break;
-        }
+        // so no thread is left behind at a later barrier.
+        const bool got = mbar_wait_bounded(&full_bar, parity, p.status);
+        parity ^= 1u;
+        if (!__syncthreads_and(got)) return;
         int x, y;
-        const bool act = node_of(t, x, y);
-        unsigned char *slot = smem + (size_t)(s * NT + tid) * p.slot_bytes;
+        const bool act = node_xy(t, x, y);
+        if (act && ((zero_mask(p, x, y) >> dir) & 1u)) zero_bytes(slot + p.d_bytes + dir * p.m_bytes, p.m_bytes);
+        __syncwarp();
+        T best = pos_inf<T>();
+        int label = 0x7fffffff;
+        if (act) belief_part<T, M, LMAX, EXACT>(p, slot, L, dir, best, label);
+        argmin_combine(best, label);
+        __syncwarp();
         if (act) {
-            const unsigned zmask = zero_mask(p, x, y);
-            T fr[FR_REGS ? LMAX : 1];
-            int label = 0;
             if (LINEAR_ONLY || p.mode == MODE_LINEAR) {
-                collect<T, M, LMAX, FR_REGS>(p, slot, zmask, fr, label);
-                messages_linear<T, M, LMAX, FR_REGS>(p, slot, zmask, fr);
+                message_linear<T, M, LMAX, EXACT>(p, slot, L, dir, scale, trunc);
             } else if constexpr (!LINEAR_ONLY) {
-                collect<T, M, LMAX, false>(p, slot, zmask, fr, label);
-                if (p.mode == MODE_REF_MINCONV) messages_ref_minconv<T, M, LMAX>(p, slot);
-                else if (p.mode == MODE_STD_MINCONV) messages_std_minconv<T, M, LMAX>(p, slot, zmask);
-                else messages_std_quad<T, M, LMAX>(p, slot, zmask);
+                if (p.mode == MODE_REF_MINCONV) messages_ref_minconv<T, M, LMAX>(p, slot, L, dir);
+                else if (p.mode == MODE_STD_MINCONV) message_std_minconv<T, M, LMAX>(p, slot, L, dir);
+                else message_std_quad<T, M, LMAX>(p, slot, L, dir, scale, trunc);
             }
-            if (p.write_labels) p.labels[(size_t)y * p.W + x] = label;
-            fence_proxy_async_shared();
-#pragma unroll
-            for (int d = 0; d < 4; ++d) {
-                const int qx = x + dir_dx(d), qy = y + dir_dy(d);
-                unsigned char *dst = p.rec + ((size_t)qy * p.W + qx) * p.rec_bytes + p.d_bytes + opp_dir(d) * p.m_bytes;
-                bulk_store(dst, slot + p.d_bytes + d * p.m_bytes, p.m_bytes);
-            }
+        }
+        // Every lane orders its shared-memory writes before the async-proxy
+        // reads of the bulk stores (lanes may store slots other lanes wrote).
+        fence_proxy_async_shared();
+        __syncwarp();
+        if (act) {
+            if (dir == 0 && p.write_labels) p.labels[(size_t)y * p.W + x] = label;
+            const int qx = x + dir_dx(dir), qy = y + dir_dy(dir);
+            unsigned char *dst =
+                p.rec + ((size_t)qy * p.W + qx) * p.rec_bytes + p.d_bytes + opp_dir(dir) * p.m_bytes;
+            bulk_store(dst, slot + p.d_bytes + dir * p.m_bytes, p.m_bytes);
             bulk_commit();
             bulk_wait_read_all();
         }
         __syncthreads();
-        const int tn = t + STAGES * gridDim.x;
-        if (tn < p.num_tiles) issue_load(tn, s);
-    }
-    if (!ok) {
-        // A copy never completed: leave without touching shared memory again.
-        return;
+        const int tn = t + gridDim.x;
+        if (tn < p.num_tiles) issue_load(tn);
     }
     bulk_wait_all();
 }
 
-template <typename T, typename M, int LMAX, int NT, int STAGES, bool LINEAR_ONLY>
-cudaError_t launch_one(const SweepParams &p, uint32_t slot_bytes, cudaStream_t s, int num_sms) {
-    auto kern = sweep_kernel<T, M, LMAX, NT, STAGES, LINEAR_ONLY>;
-    const size_t smem = (size_t)STAGES * NT * slot_bytes;
+template <typename T, typename M, int LMAX, bool EXACT, int NW, bool LINEAR_ONLY>
+cudaError_t launch_one(const SweepParams &params, uint32_t slot_bytes, cudaStream_t s, int num_sms) {
+    auto kern = sweep_kernel<T, M, LMAX, EXACT, NW, LINEAR_ONLY>;
+    // The tiling follows the variant actually launched (8*NW nodes per tile).
+    SweepParams p = params;
+    const int n1 = p.W >= 3 ? (p.W - 3) / 2 + 1 : 0;
+    p.tiles_per_row = (n1 + NW * 8 - 1) / (NW * 8);
+    p.num_tiles = p.H >= 3 ? (p.H - 2) * p.tiles_per_row : 0;
+    if (p.num_tiles <= 0) return cudaSuccess;
+    const size_t smem = (size_t)NW * 8 * slot_bytes;
     static size_t configured = 0;  // largest dynamic smem size set so far for this instantiation
     static int occ_cache_smem = -1, occ_cache = 0;
     if (smem > configured) {
@@ -553,7 +565,7 @@ cudaError_t launch_one(const SweepParams &p, uint32_t slot_bytes, cudaStream_t s
     if (occ_cache_smem == (int)smem) {
         occ = occ_cache;
     } else {
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NT, smem);
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NW * 32, smem);
         if (e != cudaSuccess) return e;
         occ_cache_smem = (int)smem;
         occ_cache = occ;
@@ -561,26 +573,25 @@ cudaError_t launch_one(const SweepParams &p, uint32_t slot_bytes, cudaStream_t s
     if (occ < 1) return cudaErrorInvalidConfiguration;
     int grid = occ * num_sms;
     if (grid > p.num_tiles) grid = p.num_tiles;
-    kern<<<grid, NT, smem, s>>>(p);
+    kern<<<grid, NW * 32, smem, s>>>(p);
     return cudaGetLastError();
 }
 
-// Dispatch on LMAX bucket and (NT, STAGES) for one (T, M) pair.  Variants
-// other than (32,1), (32,2), (64,1) fall back to (32,1).
 template <typename T, typename M, int LM>
 cudaError_t launch_variant(const RecordFormat &f, const SweepConfig &cfg, const SweepParams &p, cudaStream_t s,
                            int num_sms) {
-    if (p.mode != MODE_LINEAR) return launch_one<T, M, LM, 32, 1, false>(p, f.slot_bytes, s, num_sms);
+    if (p.mode != MODE_LINEAR) return launch_one<T, M, LM, false, 2, false>(p, f.slot_bytes, s, num_sms);
+    if (f.L != LM) return launch_one<T, M, LM, false, 2, true>(p, f.slot_bytes, s, num_sms);
     if constexpr (std::is_same<T, float>::value) {
-        if (cfg.nt == 64) return launch_one<T, M, LM, 64, 1, true>(p, f.slot_bytes, s, num_sms);
-        if (cfg.stages == 2) return launch_one<T, M, LM, 32, 2, true>(p, f.slot_bytes, s, num_sms);
+        if (cfg.nt == 8) return launch_one<T, M, LM, true, 1, true>(p, f.slot_bytes, s, num_sms);
+        if (cfg.nt == 32) return launch_one<T, M, LM, true, 4, true>(p, f.slot_bytes, s, num_sms);
     }
-    return launch_one<T, M, LM, 32, 1, true>(p, f.slot_bytes, s, num_sms);
+    return launch_one<T, M, LM, true, 2, true>(p, f.slot_bytes, s, num_sms);
 }
 
-// Dispatch on the LMAX bucket and (NT, STAGES) for one (T, M) pair.  Float
-// grids have the (32,1), (32,2) and (64,1) variants of the linear kernel;
-// everything else runs the (32,1) variant.
+// Dispatch on the LMAX bucket for one (T, M) pair.  L equal to the bucket
+// runs a kernel specialised for that L; float grids have 8-, 16- and 32-node
+// tile variants of it, everything else 16-node tiles.
 template <typename T, typename M>
 cudaError_t launch_sweep_tm(const RecordFormat &f, const SweepConfig &cfg, const SweepParams &p, cudaStream_t s,
                             int num_sms) {

@@ -77,8 +77,8 @@ typedef struct ginf_options {
     int32_t decode;          /* GINF_DECODE_*, default STALE                */
     int32_t normalize;       /* GINF_NORM_*,   default MEAN (F16 uses MIN)  */
     int32_t compute_type;    /* GINF_F32 / GINF_I32 / GINF_F64; -1 = cost_type */
-    int32_t tile_nodes;      /* nodes per sweep tile (32 or 64); 0 = tuned   */
-    int32_t stages;          /* sweep pipeline stages (1 or 2); 0 = tuned     */
+    int32_t tile_nodes;      /* nodes per sweep tile (8, 16 or 32); 0 = 16    */
+    int32_t reserved1;       /* must be 0                                     */
     int32_t reserved0;
     void *stream;            /* cudaStream_t to run on; NULL = legacy default */
     void *msgs_out;          /* optional: final level-0 messages, [H][W][4][L] of the
