@@ -39,6 +39,9 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     "hbp": dict(name="hbp_1920x1080_L64_5lvl_x10_icm5", W=1920, H=1080, L=64, levels=5, iters=10, icm=5),
     "plain": dict(name="lbp_384x288_L16_50it", W=384, H=288, L=16, levels=1, iters=50, icm=0),
+    "quad": dict(name="lbp_quad_3840x2160_L128_40it", W=3840, H=2160, L=128, levels=1, iters=40, icm=0),
+    "batch": dict(name="batch64_lbp_200x150-1280x720_L16-64_30it", W=0, H=0, L=0, levels=1, iters=30, icm=0,
+                  count=64),
 }
 METRIC = "node-label-iters/s (LBP)"
 UNIT = "node*label*iter/s"
@@ -48,6 +51,8 @@ def make_problem(kind, cfg, seed_offset=0):
     from gridinfcuda_gb300 import synth
     if kind == "hbp":
         return synth.workload_hbp(seed=1 + seed_offset, W=cfg["W"], H=cfg["H"])
+    if kind == "quad":
+        return synth.workload_quad(seed=3 + seed_offset, W=cfg["W"], H=cfg["H"], L=cfg["L"])
     return synth.workload_plain_bp(seed=0 + seed_offset, W=cfg["W"], H=cfg["H"])
 
 
@@ -307,6 +312,171 @@ def run_ours(args, cfg):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------- precision sweep
+
+def run_precision(args, cfg):
+    """Truncated-quadratic LBP (standard message rule) with the FP32 and the
+    FP16 message store, each timed, and each compared with an FP64 run of the
+    same kernels on the same input: message error (both sides re-normalised to
+    zero mean per message, max |a-b| / max |b|), label agreement on interior
+    nodes, FP64 energy gap."""
+    import torch
+    from gridinfcuda_gb300 import capi
+
+    torch.cuda.set_device(0)
+    P = make_problem("quad", cfg)
+    D = torch.from_numpy(P.D).cuda()
+    V = torch.from_numpy(P.V).cuda()
+    W, H, L, iters = cfg["W"], cfg["H"], cfg["L"], cfg["iters"]
+    ws = capi.Workspace()
+    stream = torch.cuda.current_stream()
+    base = dict(rule=capi.RULE_STANDARD, stream=stream.cuda_stream, workspace=ws)
+    nli = W * H * L * iters
+
+    def solve(store, ctype, want_msgs):
+        return capi.decode_hbp(D, V, P.model, 1, iters, want_msgs=want_msgs, want_stats=True, store=store,
+                               compute_type=ctype, **base)
+
+    def compare(msgs, lab, msgs64, lab64, e64):
+        worst, scale = 0.0, 0.0
+        for r0 in range(0, H, 64):
+            a = msgs[r0:r0 + 64].double()
+            b = msgs64[r0:r0 + 64]
+            a = a - a.mean(dim=-1, keepdim=True)
+            b = b - b.mean(dim=-1, keepdim=True)
+            worst = max(worst, float((a - b).abs().max()))
+            scale = max(scale, float(b.abs().max()))
+            del a, b
+        e = capi.energy(D, V, P.model, lab, workspace=ws)
+        return {"msg_rel_err": worst / max(scale, 1e-30),
+                "label_agreement": float((lab[1:-1, 1:-1] == lab64[1:-1, 1:-1]).double().mean()),
+                "energy": e, "energy_rel_gap": abs(e - e64) / abs(e64)}
+
+    out = {}
+    # Error against the FP64 run after 8, 16 and the configured 40 half-sweeps:
+    # loopy BP on this problem does not converge, and the gap between any two
+    # precisions grows geometrically with the iteration count.
+    curve = {"f32": {}, "f16": {}}
+    for n_it in (8, 16, iters):
+        t0 = time.perf_counter()
+        lab64, msgs64, st64 = capi.decode_hbp(D, V, P.model, 1, n_it, want_msgs=True, want_stats=True,
+                                              store=capi.STORE_NATIVE, compute_type=capi.F64, **base)
+        t64 = time.perf_counter() - t0
+        e64 = capi.energy(D, V, P.model, lab64, workspace=ws)
+        if n_it == iters:
+            out["fp64_oracle"] = {"seconds": round(t64, 2), "sweep_ms": round(st64["sweep_ms"], 2), "energy": e64}
+        for name, store in (("f32", capi.STORE_NATIVE), ("f16", capi.STORE_F16)):
+            lab, msgs, _ = capi.decode_hbp(D, V, P.model, 1, n_it, want_msgs=True, want_stats=True, store=store,
+                                           **base)
+            curve[name][n_it] = compare(msgs, lab, msgs64, lab64, e64)
+            del msgs
+        del msgs64
+        torch.cuda.empty_cache()
+    for name, store in (("f32", capi.STORE_NATIVE), ("f16", capi.STORE_F16)):
+        for _ in range(args.warmup):
+            solve(store, -1, False)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        sts = []
+        for _ in range(args.steps):
+            sts.append(solve(store, -1, False)[1])
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / args.steps
+        per_launch = sum(x["level0_sweep_ms"] for x in sts) / len(sts) / iters
+        store_b = 2 if name == "f16" else 4
+        alg = (W - 2) * (H - 2) / 2 * (L * 4 + 8 * L * store_b)
+        out[name] = dict(curve[name][iters])
+        out[name].update({"value": nli / (ms / 1e3), "unit": UNIT, "ms_per_solve": round(ms, 3),
+                          "sweep_launch_ms": round(per_launch, 4),
+                          "sweep_hbm_gbs": round(alg / (per_launch / 1e3) / 1e9, 1),
+                          "algorithmic_bytes_per_launch": alg,
+                          "vs_fp64_by_iterations": {str(k): v for k, v in curve[name].items()}})
+    peak, peak_kind = load_peaks()
+    line = {"metric": METRIC, "value": out["f16"]["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": out["f16"]["ms_per_solve"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f16 store / f32 arithmetic",
+            "data": "synthetic (seeded stereo pair, 80 slanted planar regions; no dataset)",
+            "config": {"workload": cfg["name"], "width": W, "height": H, "labels": L, "iters": iters,
+                       "smoothness": "min((a-b)^2, 25), standard message rule",
+                       "costs": "0.05 * min(|dI|, 20)"},
+            "precision": out, "peak_hbm_gbs": peak, "peak_source": peak_kind}
+    print(json.dumps(line), flush=True)
+    ws.close()
+
+
+# ---------------------------------------------------------------- batched grids
+
+def run_batch(args, cfg):
+    """64 independent grids (sizes uniform in 200x150..1280x720, L in
+    {16, 32, 64}), 30 half-sweeps each, solved by one captured batch plan
+    (persistent launches replayed from a CUDA graph, autotuned).  The cost
+    volumes are built on the GPU from seeded stereo pairs."""
+    import torch
+    from gridinfcuda_gb300 import capi, synth
+
+    rank, local, world = dist_setup(True)
+    torch.cuda.set_device(local)
+    shapes = synth.batch_shapes(cfg["count"], seed=2)
+    problems, labels, nli = [], [], 0
+    for i, (W, H, L) in enumerate(shapes):
+        pair = synth.stereo_pair(W, H, L, 12, 2.0, seed=100 + i + 1000 * rank)
+        D = torch.empty((L, H, W), dtype=torch.float32, device="cuda")
+        capi.stereo_costs(torch.from_numpy(pair.left).cuda(), torch.from_numpy(pair.right).cuda(), L, 0.07, 15.0, D)
+        V = torch.from_numpy(synth.sm_table(L, synth.TRUNC_LINEAR, 1.0, 1.7)).cuda()
+        problems.append((D, V, synth.TRUNC_LINEAR))
+        labels.append(torch.zeros((H, W), dtype=torch.int32, device="cuda"))
+        nli += W * H * L * cfg["iters"]
+    t0 = time.perf_counter()
+    plan = capi.Batch(problems, labels, cfg["iters"], autotune=1 if args.retune else 0,
+                      tile_nodes=args.tile_nodes)
+    plan_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        plan.run(stream.cuda_stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = ClockSampler(gpu_smi_id(local))
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    sts = [plan.run(stream.cuda_stream, want_stats=True) for _ in range(args.steps)]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clock_info = clocks.stop()
+    ms = reduce_max(ev0.elapsed_time(ev1), world)
+    value = world * args.steps * nli / (ms / 1e3)
+    # End to end: costs uploaded from pinned host memory, labels read back.
+    hostD = [D.cpu().pin_memory() for D, _, _ in problems]
+    hostL = [torch.empty(l.shape, dtype=torch.int32).pin_memory() for l in labels]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for (D, _, _), h in zip(problems, hostD):
+            D.copy_(h, non_blocking=True)
+        plan.run(stream.cuda_stream)
+        for l, h in zip(labels, hostL):
+            h.copy_(l, non_blocking=True)
+        torch.cuda.synchronize()
+    e2e_s = reduce_max(time.perf_counter() - t0, world)
+    h2d = sum(h.numel() * 4 for h in hostD)
+    d2h = sum(h.numel() * 4 for h in hostL)
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (64 seeded stereo pairs, cost volumes built on the GPU)",
+                "config": {"workload": cfg["name"], "grids": len(shapes), "iters": cfg["iters"],
+                           "node_label_iters_per_step": nli, "plan": plan.config(),
+                           "plan_create_s": round(plan_s, 2), "parallelism": f"replicas x{world}"},
+                "e2e": {"value": world * args.steps * nli / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_s * 1e3 / args.steps, 3)},
+                "clocks": clock_info, "gpu_launches": int(sum(s["kernel_launches"] for s in sts))}
+        print(json.dumps(line), flush=True)
+    plan.close()
+
+
 # ---------------------------------------------------------------- reference arm
 
 def run_reference(args, cfg):
@@ -349,6 +519,7 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="hbp")
     ap.add_argument("--tile-nodes", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--retune", action="store_true", help="batch workload: re-measure the autotuner's choice")
     ap.add_argument("--size", default=None, help="WxH override of the workload's grid size (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -359,6 +530,14 @@ def main():
         cfg.update(W=w, H=h, name=cfg["name"].replace(f"{cfg['W']}x{cfg['H']}", f"{w}x{h}"))
     if args.impl == "reference":
         run_reference(args, cfg)
+    elif args.workload == "batch":
+        import gridinfcuda_gb300
+        gridinfcuda_gb300.build()
+        run_batch(args, cfg)
+    elif args.workload == "quad":
+        import gridinfcuda_gb300
+        gridinfcuda_gb300.build()
+        run_precision(args, cfg)
     else:
         import gridinfcuda_gb300
         gridinfcuda_gb300.build()

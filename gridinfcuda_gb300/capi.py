@@ -38,7 +38,7 @@ class Grid(ctypes.Structure):
 
 class Options(ctypes.Structure):
     _fields_ = [("msg_rule", _i32), ("msg_store", _i32), ("decode", _i32), ("normalize", _i32),
-                ("compute_type", _i32), ("tile_nodes", _i32), ("reserved1", _i32), ("reserved0", _i32),
+                ("compute_type", _i32), ("tile_nodes", _i32), ("sweeps_per_launch", _i32), ("autotune", _i32),
                 ("stream", _p), ("msgs_out", _p), ("reserved", ctypes.c_int64 * 6)]
 
 
@@ -82,8 +82,16 @@ def lib():
         L.ginf_solve.argtypes = [_p, ctypes.POINTER(Grid), _i32, _i32, _i32, _p, ctypes.POINTER(ctypes.c_double),
                                  ctypes.POINTER(Options), ctypes.POINTER(Stats)]
         L.ginf_stereo_costs.argtypes = [_i32, _i32, _i32, _i32, _p, _p, ctypes.c_float, ctypes.c_float, _p, _p]
+        L.ginf_batch_create.argtypes = [ctypes.POINTER(_p), ctypes.POINTER(Grid), ctypes.POINTER(_p), _i32, _i32,
+                                        ctypes.POINTER(Options)]
+        L.ginf_batch_run.argtypes = [_p, _p, ctypes.POINTER(Stats)]
+        L.ginf_batch_config.argtypes = [_p, ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.POINTER(_i32)]
+        L.ginf_batch_destroy.argtypes = [_p]
+        L.ginf_decode_bp_batch.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(_p), _i32, _i32,
+                                           ctypes.POINTER(Options), ctypes.POINTER(Stats)]
         for name in ("ginf_decode_hbp", "ginf_decode_icm", "ginf_energy", "ginf_solve", "ginf_stereo_costs",
-                     "ginf_workspace_create", "ginf_workspace_destroy"):
+                     "ginf_workspace_create", "ginf_workspace_destroy", "ginf_batch_create", "ginf_batch_run",
+                     "ginf_batch_config", "ginf_batch_destroy", "ginf_decode_bp_batch"):
             getattr(L, name).restype = _i32
         _lib = L
     return _lib
@@ -159,11 +167,12 @@ def make_grid(D, V, model):
 
 
 def options(rule=RULE_REFERENCE, store=STORE_NATIVE, decode=DECODE_STALE, normalize=NORM_MEAN, compute_type=-1,
-            tile_nodes=0, stream=None, msgs_out=None):
+            tile_nodes=0, sweeps_per_launch=0, autotune=0, stream=None, msgs_out=None):
     o = Options()
     lib().ginf_default_options(ctypes.byref(o))
     o.msg_rule, o.msg_store, o.decode, o.normalize = rule, store, decode, normalize
     o.compute_type, o.tile_nodes = compute_type, tile_nodes
+    o.sweeps_per_launch, o.autotune = sweeps_per_launch, autotune
     o.stream = stream if stream is not None else None
     o.msgs_out = msgs_out
     return o
@@ -246,6 +255,48 @@ def stereo_costs(left, right, L, coef, cap, out, stream=None):
         raise ValueError("out must be a CUDA tensor")
     check(lib().ginf_stereo_costs(W, H, L, lm, lp, rp, coef, cap, op, stream))
     return out
+
+
+class Batch:
+    """A captured batch solve (``ginf_batch``): grids are (D, V, model) with
+    CUDA tensors, labels CUDA int32 tensors (H, W); run() replays the solve."""
+
+    def __init__(self, problems, labels, iters, **opt):
+        self._keep = (problems, labels)
+        n = len(problems)
+        self._grids = (Grid * n)(*[make_grid(D, V, m) for (D, V, m) in problems])
+        self._labs = (_p * n)(*[_ptr(l)[0] for l in labels])
+        self._opt = options(**opt)
+        h = _p()
+        check(lib().ginf_batch_create(ctypes.byref(h), self._grids, self._labs, n, iters, ctypes.byref(self._opt)))
+        self.handle = h
+
+    def run(self, stream=None, want_stats=False):
+        st = Stats()
+        check(lib().ginf_batch_run(self.handle, stream, ctypes.byref(st) if want_stats else None))
+        return st.as_dict() if want_stats else None
+
+    def config(self):
+        a, b, c = _i32(), _i32(), _i32()
+        check(lib().ginf_batch_config(self.handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"tile_nodes": a.value, "sweeps_per_launch": b.value, "tuned_now": bool(c.value)}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().ginf_batch_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def version() -> str:

@@ -346,10 +346,42 @@ ginf_status prepare(Call &c, Prepared &P, int levels, bool want_lab2, const int3
     return GINF_OK;
 }
 
+// Truncation radius of a quadratic table, with the comparisons of the
+// device's quad_radius (sweep_impl.cuh): V(0,k) < V(0,L-1) for k <= r on a
+// nondecreasing profile; 9 means "wider than any window".
+template <typename T>
+int quad_radius_host(const std::vector<unsigned char> &col, int L) {
+    const T *v = reinterpret_cast<const T *>(col.data());
+    const T trunc = v[L - 1];
+    int r = 0;
+    T prev = v[0];
+    for (int k = 1; k < L && k <= 9; ++k) {
+        if (v[k] < prev) return 9;
+        prev = v[k];
+        if (!(v[k] < trunc)) break;
+        r = k;
+    }
+    if (!(v[0] <= trunc)) return 9;
+    return r;
+}
+
+ginf_status table_radius(Call &c, Prepared &P, int &radius) {
+    const int L = P.f.L;
+    std::vector<unsigned char> col((size_t)L * P.f.t_size);
+    // V(0,k) = V[L*k]: one element per table row.
+    GINF_CK(cudaMemcpy2DAsync(col.data(), P.f.t_size, P.Vt, (size_t)L * P.f.t_size, P.f.t_size, L,
+                              cudaMemcpyDeviceToHost, c.r.stream));
+    GINF_CK(cudaStreamSynchronize(c.r.stream));
+    radius = P.f.ctype == CT_F64 ? quad_radius_host<double>(col, L) : quad_radius_host<float>(col, L);
+    return GINF_OK;
+}
+
 // The HBP level loop on prepared records: bp.cc:121-166 (bp.cu:180-205).
 ginf_status run_bp(Call &c, Prepared &P, int iters, int64_t &nli) {
     const RecordFormat &f = P.f;
     cudaStream_t s = c.r.stream;
+    int radius = 9;
+    if (c.r.mode == MODE_STD_QUAD) GINF_TRY(table_radius(c, P, radius));
     const int T = (int)P.lv.size();
     const bool stale = c.r.decode == GINF_DECODE_STALE;
     const int W0 = P.lv[0].W, H0 = P.lv[0].H;
@@ -404,6 +436,7 @@ ginf_status run_bp(Call &c, Prepared &P, int iters, int64_t &nli) {
         p.norm_min = c.r.norm_min;
         p.V = P.Vt;
         p.labels = P.lab;
+        p.quad_radius = radius;
         p.tiles_per_row = (n1 + c.r.cfg.nt - 1) / c.r.cfg.nt;
         p.num_tiles = (lv.H - 2) * p.tiles_per_row;
         p.status = P.status;

@@ -62,6 +62,7 @@ struct SweepParams {
     int32_t *labels;               // level-0 labels (W*H) or nullptr
     int write_labels;
     int tiles_per_row, num_tiles;  // set by the launcher for the variant it runs
+    int quad_radius;               // truncation radius of a quadratic table (kernel choice only)
     int *status;
 };
 

@@ -97,4 +97,43 @@ __device__ __forceinline__ void fence_proxy_async_shared() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// Orders this thread's async-proxy (bulk copy) and generic-proxy accesses to
+// global memory.
+__device__ __forceinline__ void fence_proxy_async_global() {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
+// Grid-wide barrier for a cooperative launch (all blocks co-resident).  bar
+// holds {arrived, generation}, zeroed before the launch.  The last block to
+// arrive resets the count and advances the generation; the others wait for
+// the generation to change, each for at most kWaitLimitNs, then record
+// DEV_ERR_TIMEOUT and report false (block-uniformly).
+__device__ __forceinline__ bool grid_barrier(unsigned int *bar, unsigned int nblocks, int *status) {
+    __syncthreads();
+    int ok = 1;
+    if (threadIdx.x == 0) {
+        volatile unsigned int *vgen = bar + 1;
+        const unsigned int gen = *vgen;
+        __threadfence();
+        const unsigned int arrived = atomicAdd(bar, 1u) + 1u;
+        if (arrived == nblocks) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            const uint64_t t0 = global_timer_ns();
+            while (*vgen == gen) {
+                __nanosleep(64);
+                if (global_timer_ns() - t0 > kWaitLimitNs) {
+                    atomicOr(status, DEV_ERR_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+    }
+    return __syncthreads_and(ok) != 0;
+}
+
 }  // namespace ginf_gpu

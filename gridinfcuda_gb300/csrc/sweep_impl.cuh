@@ -362,6 +362,104 @@ __device__ void message_std_minconv(const SweepParams &p, unsigned char *slot, i
     store_msg<T, M>(md, o, L);
 }
 
+// Largest truncation radius of the windowed quadratic transform (kernels are
+// compiled for radius 4 and radius 8 windows).
+constexpr int kQuadWindow = 8;
+constexpr int kQuadWindowSmall = 4;
+
+// Truncation radius r of a truncated-quadratic table: V(0,k) < V(0,L-1) for
+// k <= r and V(0,r+1) >= V(0,L-1).  Taps further out are dominated by
+// min(h) + V(0,L-1).  Returns kQuadWindow + 1 when r exceeds the window.
+template <typename T>
+__device__ __forceinline__ int quad_radius(const T *Vt, int L, T trunc) {
+    int r = 0;
+    T prev = __ldg(&Vt[0]);
+    for (int k = 1; k < L && k <= kQuadWindow + 1; ++k) {
+        const T v = __ldg(&Vt[(size_t)L * k]);
+        if (v < prev) return kQuadWindow + 1;  // not a nondecreasing profile: use the lower envelope
+        prev = v;
+        if (!(v < trunc)) break;
+        r = k;
+    }
+    // The profile must also start at its minimum and stay below the cap.
+    if (!(__ldg(&Vt[0]) <= trunc)) return kQuadWindow + 1;
+    return r;
+}
+
+// Standard rule, truncated quadratic, windowed exact form:
+//   out(i) = min( min_{|k| <= r} h(i+k) + V(0,|k|),  min(h) + V(0,L-1) ),
+// which equals the brute-force min_j h(j) + V(i,j) over the whole table
+// (taps beyond r cost at least min(h) + V(0,L-1)).  Branch-free, all in
+// registers: taps beyond r and labels beyond L get +inf.  With the minimum
+// subtracted, that minimum is fl(min(h) + V(0,0)) (the taps are
+// nondecreasing from V(0,0) and rounding is monotone), so each message is
+// rounded to the store type once; with the mean subtracted (FP32 store only)
+// the unnormalised values are stored exactly and corrected in a second pass.
+template <typename T, typename M, int LMAX, bool EXACT, int QW>
+__device__ __forceinline__ void message_quad_window(const SweepParams &p, unsigned char *slot, int L, int dir,
+                                                    const T *vtap, T trunc) {
+    constexpr int B = MIO<M, T>::B;
+    unsigned char *md = slot + p.d_bytes + dir * p.m_bytes;
+    T h[LMAX];
+#pragma unroll
+    for (int c = 0; c < LMAX; c += B) {
+        if (EXACT || c < L) {
+            T a[B], f[B];
+            MIO<M, T>::load(md + c * sizeof(M), a);
+            load_t<T, B>(slot + c * sizeof(T), f);
+#pragma unroll
+            for (int k = 0; k < B; ++k) h[c + k] = (EXACT || c + k < L) ? f[k] - a[k] : pos_inf<T>();
+        } else {
+#pragma unroll
+            for (int k = 0; k < B; ++k) h[c + k] = pos_inf<T>();
+        }
+    }
+    T minh = h[0];
+#pragma unroll
+    for (int i = 1; i < LMAX; ++i)
+        if (EXACT || i < L) minh = fminf(minh, h[i]);
+    const T cap = minh + trunc;
+    const bool norm_min = p.norm_min != 0;
+    const T shift = norm_min ? minh + vtap[0] : T(0);
+    T sum = T(0);
+#pragma unroll
+    for (int c = 0; c < LMAX; c += B) {
+        if (EXACT || c < L) {
+            T r[B];
+#pragma unroll
+            for (int k = 0; k < B; ++k) {
+                const int i = c + k;
+                // Symmetric taps share their cost: min(h[i-k], h[i+k]) + V(0,k)
+                // rounds exactly like the two separate sums (rounding is monotone).
+                T m = fminf(cap, h[i] + vtap[0]);
+#pragma unroll
+                for (int k2 = 1; k2 <= QW; ++k2) {
+                    const bool lo = i - k2 >= 0, hi = i + k2 < LMAX;
+                    if (lo && hi) m = fminf(m, fminf(h[i - k2], h[i + k2]) + vtap[k2]);
+                    else if (lo) m = fminf(m, h[i - k2] + vtap[k2]);
+                    else if (hi) m = fminf(m, h[i + k2] + vtap[k2]);
+                }
+                if (EXACT || i < L) sum += m;
+                r[k] = m - shift;
+            }
+            MIO<M, T>::store(md + c * sizeof(M), r);
+        }
+    }
+    if (!norm_min) {
+        const T val = mean_of<T, LMAX, EXACT>(sum, L);
+#pragma unroll
+        for (int c = 0; c < LMAX; c += B) {
+            if (EXACT || c < L) {
+                T r[B];
+                MIO<M, T>::load(md + c * sizeof(M), r);
+#pragma unroll
+                for (int k = 0; k < B; ++k) r[k] -= val;
+                MIO<M, T>::store(md + c * sizeof(M), r);
+            }
+        }
+    }
+}
+
 // Standard rule, truncated quadratic: O(L) lower envelope of parabolas
 // (Felzenszwalb & Huttenlocher, "Distance Transforms of Sampled Functions",
 // Theory of Computing 8, 2012), then truncation at min(h) + V(0, L-1).
@@ -421,9 +519,36 @@ __device__ void message_std_quad(const SweepParams &p, unsigned char *slot, int 
     }
 }
 
-// One checkerboard half-sweep.  Block = NW warps, tile = 8*NW consecutive
-// same-colour nodes of one row; lane = (node k = lane & 7, direction
-// dir = lane >> 3).  Per tile:
+enum { KIND_LINEAR = 0, KIND_QUAD = 1, KIND_GENERAL = 2, KIND_QUAD4 = 3 };
+
+// Constants a launch reads from its smoothness table: slope V(0,1) and
+// truncation V(0,L-1) (bp.cc:35,43), and for the quadratic kernels the taps
+// V(0,k) (+inf beyond the truncation radius) and that radius.
+template <typename T>
+struct TableConsts {
+    T scale, trunc;
+    T vtap[kQuadWindow + 1];
+    int qr;
+};
+
+template <typename T, int KIND>
+__device__ __forceinline__ TableConsts<T> table_consts(const void *V, int L) {
+    TableConsts<T> tc;
+    const T *Vt = static_cast<const T *>(V);
+    tc.scale = __ldg(&Vt[L]);
+    tc.trunc = __ldg(&Vt[(size_t)L * (L - 1)]);
+    tc.qr = kQuadWindow + 1;
+    if constexpr ((KIND == KIND_QUAD || KIND == KIND_QUAD4) && sizeof(T) == 4) {
+        tc.qr = quad_radius(Vt, L, tc.trunc);
+#pragma unroll
+        for (int k = 0; k <= kQuadWindow; ++k) tc.vtap[k] = k <= tc.qr ? __ldg(&Vt[(size_t)L * k]) : pos_inf<T>();
+    }
+    return tc;
+}
+
+// One tile of one checkerboard half-sweep.  Block = NW warps, tile = 8*NW
+// consecutive same-colour nodes of one row; lane = (node k = lane & 7,
+// direction dir = lane >> 3).
 //   1. lane (k, 0) brings the node's whole record into the node's padded
 //      shared-memory slot with one bulk TMA copy (complete_tx on the
 //      block's mbarrier; the first sweep of a level fetches D and, per lane,
@@ -435,118 +560,155 @@ __device__ void message_std_quad(const SweepParams &p, unsigned char *slot, int 
 //      OPP(dir).
 // Lanes 0-7 of a warp are eight different nodes with the same direction; the
 // odd slot stride in 16-byte chunks puts their 128-bit shared accesses in
-// eight different bank groups.
-template <typename T, typename M, int LMAX, bool EXACT, int NW, bool LINEAR_ONLY>
+// eight different bank groups.  KIND selects the message rule compiled in:
+// the truncated-linear update only (the hot path, with a clean register
+// allocation), the standard truncated-quadratic update (window radius 8, or
+// 4 for KIND_QUAD4), or every rule.  Returns false, block-uniformly, when the
+// bounded wait for the tile's copies gave up.
+template <int NW>
+__device__ __forceinline__ bool tile_node(const SweepParams &p, int t, int &x, int &y) {
+    const int node = (threadIdx.x >> 5) * 8 + (threadIdx.x & 7);
+    y = 1 + t / p.tiles_per_row;
+    x = ((y + p.iter) & 1) + 1 + 2 * ((t % p.tiles_per_row) * NW * 8 + node);
+    return x <= p.W - 2;
+}
+
+// Phase 1 of a tile: every thread announces the bytes it will receive on the
+// block's mbarrier, then lane (k, 0) brings the node's whole record into the
+// node's padded shared-memory slot with one bulk TMA copy (the first sweep of
+// a level fetches D and, per lane, one incoming slot from the coarser level
+// instead).
+template <int NW>
+__device__ __forceinline__ void tile_load(const SweepParams &p, int t, unsigned char *smem, uint64_t *bar) {
+    const int dir = (threadIdx.x & 31) >> 3;
+    const int node = (threadIdx.x >> 5) * 8 + (threadIdx.x & 7);
+    unsigned char *slot = smem + (size_t)node * p.slot_bytes;
+    int x, y;
+    const bool act = tile_node<NW>(p, t, x, y);
+    uint32_t bytes = 0;
+    bool want = false;
+    if (act) {
+        if (p.read_mode == RD_OWN) {
+            if (dir == 0) bytes = p.rec_bytes;
+        } else {
+            if (dir == 0) bytes = p.d_bytes;
+            if (p.read_mode == RD_COARSE) {
+                want = !((zero_mask(p, x, y) >> dir) & 1u);
+                if (want) bytes += p.m_bytes;
+            }
+        }
+    }
+    mbar_arrive_expect_tx(bar, bytes);
+    if (act) {
+        const unsigned char *r = p.rec + ((size_t)y * p.W + x) * p.rec_bytes;
+        if (p.read_mode == RD_OWN) {
+            if (dir == 0) bulk_load(slot, r, p.rec_bytes, bar);
+        } else {
+            if (dir == 0) bulk_load(slot, r, p.d_bytes, bar);
+            if (want) {
+                // The coarse node Q = (node + dir) / 2 sent its message towards
+                // -dir; it is stored at R = Q - dir, slot dir.
+                const int Qx = (x + dir_dx(dir)) >> 1, Qy = (y + dir_dy(dir)) >> 1;
+                const int Rx = Qx - dir_dx(dir), Ry = Qy - dir_dy(dir);
+                const unsigned char *src = p.crec + ((size_t)Ry * p.cW + Rx) * p.rec_bytes + p.d_bytes + dir * p.m_bytes;
+                bulk_load(slot + p.d_bytes + dir * p.m_bytes, src, p.m_bytes, bar);
+            }
+        }
+    }
+}
+
+// Phase 2 of a tile (lane = (node k = lane & 7, direction dir = lane >> 3)):
+//   wait for the copies (bounded; the vote makes giving up block-uniform, so
+//   no thread is left behind at a later barrier -- returns false then);
+//   zero incoming slots whose sender is a border node; the node's four lanes
+//   form the belief over D and its first argmin; lane (k, dir) forms the
+//   message towards dir over its incoming slot and bulk-stores it into the
+//   neighbour's record, slot OPP(dir).
+// Lanes 0-7 of a warp are eight different nodes with the same direction; the
+// odd slot stride in 16-byte chunks puts their 128-bit shared accesses in
+// eight different bank groups.  KIND selects the message rule compiled in:
+// the truncated-linear update only (the hot path, with a clean register
+// allocation), the standard truncated-quadratic update (window radius 8, or
+// 4 for KIND_QUAD4), or every rule.
+template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND>
+__device__ __forceinline__ bool tile_finish(const SweepParams &p, const TableConsts<T> &tc, int t,
+                                            unsigned char *smem, uint64_t *bar, uint32_t &parity) {
+    const int dir = (threadIdx.x & 31) >> 3;
+    const int node = (threadIdx.x >> 5) * 8 + (threadIdx.x & 7);
+    const int L = EXACT ? LMAX : p.L;
+    unsigned char *slot = smem + (size_t)node * p.slot_bytes;
+    const bool got = mbar_wait_bounded(bar, parity, p.status);
+    parity ^= 1u;
+    if (!__syncthreads_and(got)) return false;
+    int x, y;
+    const bool act = tile_node<NW>(p, t, x, y);
+    if (act && ((zero_mask(p, x, y) >> dir) & 1u)) zero_bytes(slot + p.d_bytes + dir * p.m_bytes, p.m_bytes);
+    __syncwarp();
+    T best = pos_inf<T>();
+    int label = 0x7fffffff;
+    if (act) belief_part<T, M, LMAX, EXACT>(p, slot, L, dir, best, label);
+    argmin_combine(best, label);
+    __syncwarp();
+    if (act) {
+        if constexpr (KIND == KIND_LINEAR) {
+            message_linear<T, M, LMAX, EXACT>(p, slot, L, dir, tc.scale, tc.trunc);
+        } else if constexpr (KIND == KIND_QUAD || KIND == KIND_QUAD4) {
+            constexpr int QW = KIND == KIND_QUAD4 ? kQuadWindowSmall : kQuadWindow;
+            if constexpr (sizeof(T) == 4 && !std::is_same<T, int>::value) {
+                if (tc.qr <= QW) message_quad_window<T, M, LMAX, EXACT, QW>(p, slot, L, dir, tc.vtap, tc.trunc);
+                else message_std_quad<T, M, LMAX>(p, slot, L, dir, tc.scale, tc.trunc);
+            } else {
+                message_std_quad<T, M, LMAX>(p, slot, L, dir, tc.scale, tc.trunc);
+            }
+        } else {
+            if (p.mode == MODE_LINEAR) message_linear<T, M, LMAX, EXACT>(p, slot, L, dir, tc.scale, tc.trunc);
+            else if (p.mode == MODE_REF_MINCONV) messages_ref_minconv<T, M, LMAX>(p, slot, L, dir);
+            else if (p.mode == MODE_STD_MINCONV) message_std_minconv<T, M, LMAX>(p, slot, L, dir);
+            else message_std_quad<T, M, LMAX>(p, slot, L, dir, tc.scale, tc.trunc);
+        }
+    }
+    // Every lane orders its shared-memory writes before the async-proxy
+    // reads of the bulk stores (lanes may store slots other lanes wrote).
+    fence_proxy_async_shared();
+    __syncwarp();
+    if (act) {
+        if (dir == 0 && p.write_labels) p.labels[(size_t)y * p.W + x] = label;
+        const int qx = x + dir_dx(dir), qy = y + dir_dy(dir);
+        unsigned char *dst = p.rec + ((size_t)qy * p.W + qx) * p.rec_bytes + p.d_bytes + opp_dir(dir) * p.m_bytes;
+        bulk_store(dst, slot + p.d_bytes + dir * p.m_bytes, p.m_bytes);
+        bulk_commit();
+        bulk_wait_read_all();
+    }
+    __syncthreads();
+    return true;
+}
+
+// One checkerboard half-sweep of one level: blocks take tiles in turn, each
+// issuing the copies of its next tile as soon as the current one is done.
+template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND>
 __global__ void __launch_bounds__(NW * 32) sweep_kernel(const SweepParams p) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t full_bar;
-    constexpr int NN = NW * 8;
-    const int tid = threadIdx.x, lane = tid & 31;
-    const int dir = lane >> 3;
-    const int node = (tid >> 5) * 8 + (lane & 7);
-    const int L = EXACT ? LMAX : p.L;
-    unsigned char *slot = smem + (size_t)node * p.slot_bytes;
-    const T *Vt = static_cast<const T *>(p.V);
-    const T scale = __ldg(&Vt[L]), trunc = __ldg(&Vt[(size_t)L * (L - 1)]);  // V(0,1), V(0,L-1): bp.cc:35,43
-    if (tid == 0) {
+    const TableConsts<T> tc = table_consts<T, KIND>(p.V, EXACT ? LMAX : p.L);
+    if (threadIdx.x == 0) {
         mbar_init(&full_bar, NW * 32);
         fence_barrier_init();
     }
     __syncthreads();
-
-    auto node_xy = [&](int t, int &x, int &y) -> bool {
-        y = 1 + t / p.tiles_per_row;
-        const int kk = (t % p.tiles_per_row) * NN + node;
-        x = ((y + p.iter) & 1) + 1 + 2 * kk;
-        return x <= p.W - 2;
-    };
-
-    auto issue_load = [&](int t) {
-        int x, y;
-        const bool act = node_xy(t, x, y);
-        uint32_t bytes = 0;
-        bool want = false;
-        if (act) {
-            if (p.read_mode == RD_OWN) {
-                if (dir == 0) bytes = p.rec_bytes;
-            } else {
-                if (dir == 0) bytes = p.d_bytes;
-                if (p.read_mode == RD_COARSE) {
-                    want = !((zero_mask(p, x, y) >> dir) & 1u);
-                    if (want) bytes += p.m_bytes;
-                }
-            }
-        }
-        mbar_arrive_expect_tx(&full_bar, bytes);
-        if (act) {
-            const unsigned char *r = p.rec + ((size_t)y * p.W + x) * p.rec_bytes;
-            if (p.read_mode == RD_OWN) {
-                if (dir == 0) bulk_load(slot, r, p.rec_bytes, &full_bar);
-            } else {
-                if (dir == 0) bulk_load(slot, r, p.d_bytes, &full_bar);
-                if (want) {
-                    // The coarse node Q = (node + dir) / 2 sent its message towards
-                    // -dir; it is stored at R = Q - dir, slot dir.
-                    const int Qx = (x + dir_dx(dir)) >> 1, Qy = (y + dir_dy(dir)) >> 1;
-                    const int Rx = Qx - dir_dx(dir), Ry = Qy - dir_dy(dir);
-                    const unsigned char *src =
-                        p.crec + ((size_t)Ry * p.cW + Rx) * p.rec_bytes + p.d_bytes + dir * p.m_bytes;
-                    bulk_load(slot + p.d_bytes + dir * p.m_bytes, src, p.m_bytes, &full_bar);
-                }
-            }
-        }
-    };
-
     int t = blockIdx.x;
-    if (t < p.num_tiles) issue_load(t);
+    if (t < p.num_tiles) tile_load<NW>(p, t, smem, &full_bar);
     uint32_t parity = 0;
     for (; t < p.num_tiles; t += gridDim.x) {
-        // Every thread's wait is bounded; the vote makes giving up block-uniform
-        // so no thread is left behind at a later barrier.
-        const bool got = mbar_wait_bounded(&full_bar, parity, p.status);
-        parity ^= 1u;
-        if (!__syncthreads_and(got)) return;
-        int x, y;
-        const bool act = node_xy(t, x, y);
-        if (act && ((zero_mask(p, x, y) >> dir) & 1u)) zero_bytes(slot + p.d_bytes + dir * p.m_bytes, p.m_bytes);
-        __syncwarp();
-        T best = pos_inf<T>();
-        int label = 0x7fffffff;
-        if (act) belief_part<T, M, LMAX, EXACT>(p, slot, L, dir, best, label);
-        argmin_combine(best, label);
-        __syncwarp();
-        if (act) {
-            if (LINEAR_ONLY || p.mode == MODE_LINEAR) {
-                message_linear<T, M, LMAX, EXACT>(p, slot, L, dir, scale, trunc);
-            } else if constexpr (!LINEAR_ONLY) {
-                if (p.mode == MODE_REF_MINCONV) messages_ref_minconv<T, M, LMAX>(p, slot, L, dir);
-                else if (p.mode == MODE_STD_MINCONV) message_std_minconv<T, M, LMAX>(p, slot, L, dir);
-                else message_std_quad<T, M, LMAX>(p, slot, L, dir, scale, trunc);
-            }
-        }
-        // Every lane orders its shared-memory writes before the async-proxy
-        // reads of the bulk stores (lanes may store slots other lanes wrote).
-        fence_proxy_async_shared();
-        __syncwarp();
-        if (act) {
-            if (dir == 0 && p.write_labels) p.labels[(size_t)y * p.W + x] = label;
-            const int qx = x + dir_dx(dir), qy = y + dir_dy(dir);
-            unsigned char *dst =
-                p.rec + ((size_t)qy * p.W + qx) * p.rec_bytes + p.d_bytes + opp_dir(dir) * p.m_bytes;
-            bulk_store(dst, slot + p.d_bytes + dir * p.m_bytes, p.m_bytes);
-            bulk_commit();
-            bulk_wait_read_all();
-        }
-        __syncthreads();
+        if (!tile_finish<T, M, LMAX, EXACT, NW, KIND>(p, tc, t, smem, &full_bar, parity)) return;
         const int tn = t + gridDim.x;
-        if (tn < p.num_tiles) issue_load(tn);
+        if (tn < p.num_tiles) tile_load<NW>(p, tn, smem, &full_bar);
     }
     bulk_wait_all();
 }
 
-template <typename T, typename M, int LMAX, bool EXACT, int NW, bool LINEAR_ONLY>
+template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND>
 cudaError_t launch_one(const SweepParams &params, uint32_t slot_bytes, cudaStream_t s, int num_sms) {
-    auto kern = sweep_kernel<T, M, LMAX, EXACT, NW, LINEAR_ONLY>;
+    auto kern = sweep_kernel<T, M, LMAX, EXACT, NW, KIND>;
     // The tiling follows the variant actually launched (8*NW nodes per tile).
     SweepParams p = params;
     const int n1 = p.W >= 3 ? (p.W - 3) / 2 + 1 : 0;
@@ -580,13 +742,24 @@ cudaError_t launch_one(const SweepParams &params, uint32_t slot_bytes, cudaStrea
 template <typename T, typename M, int LM>
 cudaError_t launch_variant(const RecordFormat &f, const SweepConfig &cfg, const SweepParams &p, cudaStream_t s,
                            int num_sms) {
-    if (p.mode != MODE_LINEAR) return launch_one<T, M, LM, false, 2, false>(p, f.slot_bytes, s, num_sms);
-    if (f.L != LM) return launch_one<T, M, LM, false, 2, true>(p, f.slot_bytes, s, num_sms);
-    if constexpr (std::is_same<T, float>::value) {
-        if (cfg.nt == 8) return launch_one<T, M, LM, true, 1, true>(p, f.slot_bytes, s, num_sms);
-        if (cfg.nt == 32) return launch_one<T, M, LM, true, 4, true>(p, f.slot_bytes, s, num_sms);
+    const bool exact = f.L == LM;
+    if (p.mode == MODE_STD_QUAD) {
+        // The host measured the truncation radius (quad_radius_host); radius-4
+        // windows run the cheaper 9-tap kernel.
+        if (p.quad_radius <= kQuadWindowSmall) {
+            if (exact) return launch_one<T, M, LM, true, 2, KIND_QUAD4>(p, f.slot_bytes, s, num_sms);
+            return launch_one<T, M, LM, false, 2, KIND_QUAD4>(p, f.slot_bytes, s, num_sms);
+        }
+        if (exact) return launch_one<T, M, LM, true, 2, KIND_QUAD>(p, f.slot_bytes, s, num_sms);
+        return launch_one<T, M, LM, false, 2, KIND_QUAD>(p, f.slot_bytes, s, num_sms);
     }
-    return launch_one<T, M, LM, true, 2, true>(p, f.slot_bytes, s, num_sms);
+    if (p.mode != MODE_LINEAR) return launch_one<T, M, LM, false, 2, KIND_GENERAL>(p, f.slot_bytes, s, num_sms);
+    if (!exact) return launch_one<T, M, LM, false, 2, KIND_LINEAR>(p, f.slot_bytes, s, num_sms);
+    if constexpr (std::is_same<T, float>::value) {
+        if (cfg.nt == 8) return launch_one<T, M, LM, true, 1, KIND_LINEAR>(p, f.slot_bytes, s, num_sms);
+        if (cfg.nt == 32) return launch_one<T, M, LM, true, 4, KIND_LINEAR>(p, f.slot_bytes, s, num_sms);
+    }
+    return launch_one<T, M, LM, true, 2, KIND_LINEAR>(p, f.slot_bytes, s, num_sms);
 }
 
 // Dispatch on the LMAX bucket for one (T, M) pair.  L equal to the bucket

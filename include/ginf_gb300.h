@@ -77,9 +77,12 @@ typedef struct ginf_options {
     int32_t decode;          /* GINF_DECODE_*, default STALE                */
     int32_t normalize;       /* GINF_NORM_*,   default MEAN (F16 uses MIN)  */
     int32_t compute_type;    /* GINF_F32 / GINF_I32 / GINF_F64; -1 = cost_type */
-    int32_t tile_nodes;      /* nodes per sweep tile (8, 16 or 32); 0 = 16    */
-    int32_t reserved1;       /* must be 0                                     */
-    int32_t reserved0;
+    int32_t tile_nodes;      /* nodes per sweep tile (8, 16 or 32); 0 = default
+                                (16), or the autotuned choice for batches        */
+    int32_t sweeps_per_launch; /* batches: half-sweeps per persistent launch;
+                                  0 = autotuned                                */
+    int32_t autotune;        /* batches: 0 = cached choice, else measure and cache;
+                                1 = always measure; -1 = never (defaults)        */
     void *stream;            /* cudaStream_t to run on; NULL = legacy default */
     void *msgs_out;          /* optional: final level-0 messages, [H][W][4][L] of the
                                 compute type, slot d = message from the neighbour in
@@ -161,6 +164,34 @@ ginf_status ginf_solve(ginf_workspace *ws, const ginf_grid *grid, int32_t num_le
 ginf_status ginf_stereo_costs(int32_t width, int32_t height, int32_t num_labels, int32_t memory,
                               const float *left, const float *right, float coef, float cap,
                               float *costs, void *stream);
+
+/* Batches: many independent grids, each solved by loopy BP (one level,
+ * `iters` half-sweeps, the reference's semantics and stale-belief decode, as
+ * ginf_decode_hbp with num_levels == 1).  The reference solves one grid per
+ * call (src/include/bp.h:14-26); a batch solves them together in one
+ * persistent cooperative launch per `sweeps_per_launch` half-sweeps, walking
+ * a work list of (grid, tile) tickets, and replays the whole solve from a
+ * CUDA graph captured at creation.  Grids: FP32 costs, Potts or
+ * truncated-linear smoothness, 2 <= L <= 64, all buffers device memory; the
+ * plan keeps the pointers, so later runs see whatever those buffers hold.
+ * The tile size and half-sweeps per launch are given in `opt` or chosen by
+ * the autotuner, which times the candidates on this batch and caches the
+ * winner per mix of (label count, log2 node count) buckets in the JSON file
+ * named by $GINF_AUTOTUNE_CACHE (default
+ * $XDG_CACHE_HOME or ~/.cache/gridinfcuda_gb300_autotune.json). */
+typedef struct ginf_batch ginf_batch;
+ginf_status ginf_batch_create(ginf_batch **batch, const ginf_grid *grids, int32_t *const *labels, int32_t count,
+                              int32_t iters, const ginf_options *opt);
+/* Replays the captured solve on `stream` (cudaStream_t) and waits for it. */
+ginf_status ginf_batch_run(ginf_batch *batch, void *stream, ginf_stats *stats);
+/* The tile size and half-sweeps per launch in use, and whether this plan
+ * measured them (1) or took them from the options or the cache (0). */
+ginf_status ginf_batch_config(const ginf_batch *batch, int32_t *tile_nodes, int32_t *sweeps_per_launch,
+                              int32_t *tuned_now);
+ginf_status ginf_batch_destroy(ginf_batch *batch);
+/* Create, run once, destroy. */
+ginf_status ginf_decode_bp_batch(const ginf_grid *grids, int32_t *const *labels, int32_t count, int32_t iters,
+                                 const ginf_options *opt, ginf_stats *stats);
 
 /* Loopy BP (one level, the reference message rule and stale-belief decode)
  * that allocates no device memory.  It has no counterpart in the reference.

@@ -1,0 +1,107 @@
+"""Batched loopy BP (one persistent launch per group of half-sweeps, replayed
+from a CUDA graph): every grid's labels must equal a single-grid solve of
+the same grid, bit for bit, for every tile size and half-sweeps-per-launch."""
+import os
+
+import numpy as np
+import pytest
+
+from gridinfcuda_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(37, 29, 16), (64, 40, 32), (23, 61, 64), (50, 50, 24), (3, 7, 16), (129, 17, 16), (8, 3, 32),
+          (70, 45, 64)]
+
+
+def _problems(seed0=0):
+    import torch
+    out = []
+    for i, (W, H, L) in enumerate(SHAPES):
+        model = synth.POTTS if i % 3 == 2 else synth.TRUNC_LINEAR
+        P = synth.random_problem(W, H, L, seed0 + i, model=model, scale=0.7 if model == synth.POTTS else 1.0,
+                                 trunc=2.5)
+        out.append((torch.from_numpy(P.D).cuda(), torch.from_numpy(P.V).cuda(), P.model))
+    return out
+
+
+def _single(ginf, problems, iters):
+    import torch
+    res = []
+    for D, V, m in problems:
+        lab = torch.zeros(D.shape[1:], dtype=torch.int32, device="cuda")
+        res.append(ginf.decode_hbp(D, V, m, 1, iters, labels=lab).cpu().numpy())
+    return res
+
+
+@pytest.mark.parametrize("tile,spl", [(8, 1), (16, 0), (32, 3), (16, 5), (8, 0)])
+def test_batch_equals_single_grid_solves(ginf, tile, spl):
+    import torch
+    problems = _problems()
+    iters = 11
+    want = _single(ginf, problems, iters)
+    labels = [torch.zeros(D.shape[1:], dtype=torch.int32, device="cuda") for D, _, _ in problems]
+    with ginf.Batch(problems, labels, iters, tile_nodes=tile, sweeps_per_launch=spl) as b:
+        assert b.config()["tuned_now"] is False
+        for rep in range(2):
+            b.run()
+            for g, (lab, w) in enumerate(zip(labels, want)):
+                assert np.array_equal(lab.cpu().numpy(), w), (tile, spl, rep, g)
+
+
+@pytest.mark.parametrize("iters", [0, 1, 2])
+def test_batch_short_runs(ginf, iters):
+    import torch
+    problems = _problems(50)
+    want = _single(ginf, problems, iters)
+    labels = [torch.zeros(D.shape[1:], dtype=torch.int32, device="cuda") for D, _, _ in problems]
+    with ginf.Batch(problems, labels, iters, tile_nodes=16, sweeps_per_launch=0) as b:
+        b.run()
+    for lab, w in zip(labels, want):
+        assert np.array_equal(lab.cpu().numpy(), w)
+
+
+def test_batch_replay_sees_new_costs(ginf):
+    import torch
+    problems = _problems(7)
+    labels = [torch.zeros(D.shape[1:], dtype=torch.int32, device="cuda") for D, _, _ in problems]
+    with ginf.Batch(problems, labels, 9, tile_nodes=16, sweeps_per_launch=0) as b:
+        b.run()
+        fresh = _problems(99)
+        for (D, V, _), (D2, V2, _) in zip(problems, fresh):
+            D.copy_(D2)
+            V.copy_(V2)
+        b.run()
+    want = _single(ginf, fresh, 9)
+    for lab, w in zip(labels, want):
+        assert np.array_equal(lab.cpu().numpy(), w)
+
+
+def test_autotuner_measures_then_uses_its_cache(ginf, tmp_path, monkeypatch):
+    import torch
+    monkeypatch.setenv("GINF_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    problems = _problems(3)
+    want = _single(ginf, problems, 8)
+    labels = [torch.zeros(D.shape[1:], dtype=torch.int32, device="cuda") for D, _, _ in problems]
+    with ginf.Batch(problems, labels, 8) as b:
+        c1 = b.config()
+        b.run()
+    assert c1["tuned_now"] is True
+    assert os.path.exists(tmp_path / "tune.json")
+    assert '"tile_nodes"' in open(tmp_path / "tune.json").read()
+    for lab, w in zip(labels, want):
+        assert np.array_equal(lab.cpu().numpy(), w)
+    with ginf.Batch(problems, labels, 8) as b:
+        c2 = b.config()
+    assert c2["tuned_now"] is False
+    assert (c2["tile_nodes"], c2["sweeps_per_launch"]) == (c1["tile_nodes"], c1["sweeps_per_launch"])
+
+
+def test_batch_rejects_unsupported_grids(ginf):
+    import torch
+    P = synth.random_problem(20, 20, 80, 1)
+    D, V = torch.from_numpy(P.D).cuda(), torch.from_numpy(P.V).cuda()
+    lab = torch.zeros((20, 20), dtype=torch.int32, device="cuda")
+    with pytest.raises(ginf.GinfError) as e:
+        ginf.Batch([(D, V, P.model)], [lab], 4)
+    assert e.value.status == ginf.ERR_UNSUPPORTED

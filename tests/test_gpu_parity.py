@@ -137,9 +137,11 @@ def test_fp64_path_matches_fp64_oracle(ginf, orc):
 
 
 def test_standard_quadratic_fp32_and_fp16_vs_fp64_oracle(ginf, orc):
-    """Truncated-quadratic standard BP (O(L) lower envelope): FP32 store within
-    1e-4 relative of the FP64 oracle, FP16 store within 5e-3; labels agree on
-    >= 99.9% (FP32) and >= 99% (FP16) of nodes; energies within 1e-5 / 1e-3."""
+    """Truncated-quadratic standard BP against the FP64 oracle: messages within
+    1e-4 (FP32 store) / 5e-3 (FP16 store) relative; labels agree on >= 99.9% /
+    99% of nodes.  Energies within 1e-3 / 5e-3: one label flip at a near-tie
+    moves this 96x72 grid's energy by an integer table step (4 / 14174 =
+    2.8e-4), so the bound allows a few flips."""
     P = synth.stereo_problem(96, 72, 32, seed=4, n_regions=10, sigma=3.0, planar=True, coef=0.05, cap=20.0,
                              model=synth.TRUNC_QUAD, scale=1.0, trunc=25.0)
     want, mw = orc.hbp_f64_std(P.D, P.V, P.model, 1, 12, want_msgs=True)
@@ -147,13 +149,13 @@ def test_standard_quadratic_fp32_and_fp16_vs_fp64_oracle(ginf, orc):
     f32, m32 = ginf.decode_hbp(P.D, P.V, P.model, 1, 12, want_msgs=True, rule=ginf.RULE_STANDARD)
     assert _msg_rel_err(m32, mw) < 1e-4
     assert (f32[1:-1, 1:-1] == want[1:-1, 1:-1]).mean() >= 0.999
-    assert abs(orc.energy(P.D, P.V, f32) - e_want) / abs(e_want) < 1e-5
+    assert abs(orc.energy(P.D, P.V, f32) - e_want) / abs(e_want) < 1e-3
     _, mw_min = orc.hbp_f64_std(P.D, P.V, P.model, 1, 12, norm=1, want_msgs=True)
     f16, m16 = ginf.decode_hbp(P.D, P.V, P.model, 1, 12, want_msgs=True, rule=ginf.RULE_STANDARD,
                                store=ginf.STORE_F16)
     assert _msg_rel_err(m16, mw_min) < 5e-3
     assert (f16[1:-1, 1:-1] == want[1:-1, 1:-1]).mean() >= 0.99
-    assert abs(orc.energy(P.D, P.V, f16) - e_want) / abs(e_want) < 1e-3
+    assert abs(orc.energy(P.D, P.V, f16) - e_want) / abs(e_want) < 5e-3
 
 
 def test_fp16_store_linear_vs_fp64(ginf, orc):
@@ -232,3 +234,24 @@ def test_errors_are_reported_not_fatal(ginf):
     # the library stays usable after the errors
     lab = ginf.decode_hbp(P.D, P.V, P.model, 1, 3)
     assert lab.shape == (8, 10)
+
+
+def test_windowed_quadratic_equals_min_convolution(ginf):
+    """The windowed truncated-quadratic transform is the exact minimum over the
+    whole table: bit-identical to the O(L^2) min-convolution of the same table."""
+    for L, trunc in ((128, 25.0), (17, 9.0), (64, 2.0)):
+        P = synth.random_problem(37, 23, L, 40 + L, model=synth.TRUNC_QUAD, scale=1.0, trunc=trunc, cost_max=30.0)
+        lq, mq = ginf.decode_hbp(P.D, P.V, synth.TRUNC_QUAD, 2, 5, want_msgs=True, rule=ginf.RULE_STANDARD)
+        lb, mb = ginf.decode_hbp(P.D, P.V, synth.EXPLICIT, 2, 5, want_msgs=True, rule=ginf.RULE_STANDARD)
+        assert np.array_equal(lq, lb), L
+        assert np.array_equal(mq.view(np.uint32), mb.view(np.uint32)), L
+
+
+def test_wide_quadratic_lower_envelope_vs_fp64(ginf, orc):
+    """Truncation radius beyond the window (s = 0.05, d = 25: radius 22): the
+    lower-envelope transform, FP32 store within 1e-4 of the FP64 oracle."""
+    P = synth.random_problem(41, 31, 64, 9, model=synth.TRUNC_QUAD, scale=0.05, trunc=25.0, cost_max=30.0)
+    want, mw = orc.hbp_f64_std(P.D, P.V, P.model, 1, 8, want_msgs=True)
+    got, mg = ginf.decode_hbp(P.D, P.V, P.model, 1, 8, want_msgs=True, rule=ginf.RULE_STANDARD)
+    assert _msg_rel_err(mg, mw) < 1e-4
+    assert (got[1:-1, 1:-1] == want[1:-1, 1:-1]).mean() >= 0.999
