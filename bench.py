@@ -40,6 +40,7 @@ WORKLOADS = {
     "hbp": dict(name="hbp_1920x1080_L64_5lvl_x10_icm5", W=1920, H=1080, L=64, levels=5, iters=10, icm=5),
     "plain": dict(name="lbp_384x288_L16_50it", W=384, H=288, L=16, levels=1, iters=50, icm=0),
     "quad": dict(name="lbp_quad_3840x2160_L128_40it", W=3840, H=2160, L=128, levels=1, iters=40, icm=0),
+    "warm": dict(name="learned_warm_start_hbp_1920x1080_L64", W=1920, H=1080, L=64, levels=5, iters=0, icm=0),
     "batch": dict(name="batch64_lbp_200x150-1280x720_L16-64_30it", W=0, H=0, L=0, levels=1, iters=30, icm=0,
                   count=64),
 }
@@ -477,6 +478,45 @@ def run_batch(args, cfg):
     plan.close()
 
 
+# ---------------------------------------------------------------- learned warm start
+
+def run_warm(args, cfg):
+    """Train the warm-start network on converged BP messages of seeded
+    512x384x64 grids with the library's own tensor-core kernels, then measure
+    time to energy (within 0.5 % of converged plain HBP) warm vs cold on
+    unseen 1920x1080x64 grids."""
+    import torch
+    from gridinfcuda_gb300 import capi, warmstart
+
+    torch.cuda.set_device(0)
+    log = (lambda m: print(m, file=sys.stderr, flush=True)) if args.verbose else None
+    t0 = time.perf_counter()
+    X, Y = warmstart.make_training_set(n=args.train_grids, level=args.warm_level)
+    t_data = time.perf_counter() - t0
+    net = capi.WarmNet(64, 32, seed=1)
+    t0 = time.perf_counter()
+    hist = warmstart.train(net, X, Y, epochs=args.epochs, batch=args.batch, lr=args.lr, log=log)
+    t_train = time.perf_counter() - t0
+    if args.save_net:
+        net.save(args.save_net)
+    base_loss = float(((X - Y) ** 2).mean())   # loss of the network-free guess y = x
+    del X, Y
+    torch.cuda.empty_cache()
+    res = warmstart.evaluate(net, n=args.eval_grids, log=log, level=args.warm_level)
+    summ = warmstart.summarize(res)
+    line = {"metric": "ms to plain-BP energy +0.5%, warm-start vs plain", "value": summ["ms_warm_mean"],
+            "unit": "ms", "n_gpus": 1, "higher_is_better": False, "vs_baseline": None, "dtype": "bf16 net / f32 BP",
+            "data": "synthetic (seeded planar-region stereo; no dataset)",
+            "config": {"workload": cfg["name"], "train_grids": args.train_grids, "train_size": "512x384x64",
+                       "eval_grids": args.eval_grids, "epochs": args.epochs, "levels": 5,
+                       "warm_level": args.warm_level, "batch": args.batch, "lr": args.lr},
+            "warm_start": summ,
+            "training": {"data_s": round(t_data, 1), "train_s": round(t_train, 1), "final_loss": hist[-1],
+                         "first_epoch_loss": hist[0], "loss_without_network": base_loss}}
+    print(json.dumps(line), flush=True)
+    net.close()
+
+
 # ---------------------------------------------------------------- reference arm
 
 def run_reference(args, cfg):
@@ -519,6 +559,14 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="hbp")
     ap.add_argument("--tile-nodes", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--train-grids", type=int, default=2000, help="warm workload: training grids")
+    ap.add_argument("--eval-grids", type=int, default=256, help="warm workload: evaluation grids")
+    ap.add_argument("--epochs", type=int, default=30, help="warm workload: training epochs")
+    ap.add_argument("--save-net", default=None, help="warm workload: write the trained network here")
+    ap.add_argument("--warm-level", type=int, default=1, help="warm workload: pyramid level the network seeds")
+    ap.add_argument("--batch", type=int, default=32, help="warm workload: training batch (images)")
+    ap.add_argument("--lr", type=float, default=2e-3, help="warm workload: Adam learning rate")
+    ap.add_argument("--verbose", action="store_true")
     ap.add_argument("--retune", action="store_true", help="batch workload: re-measure the autotuner's choice")
     ap.add_argument("--size", default=None, help="WxH override of the workload's grid size (profiling runs)")
     args = ap.parse_args()
@@ -530,6 +578,10 @@ def main():
         cfg.update(W=w, H=h, name=cfg["name"].replace(f"{cfg['W']}x{cfg['H']}", f"{w}x{h}"))
     if args.impl == "reference":
         run_reference(args, cfg)
+    elif args.workload == "warm":
+        import gridinfcuda_gb300
+        gridinfcuda_gb300.build()
+        run_warm(args, cfg)
     elif args.workload == "batch":
         import gridinfcuda_gb300
         gridinfcuda_gb300.build()

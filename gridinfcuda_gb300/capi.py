@@ -46,7 +46,7 @@ class Stats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in ("total_ms", "upload_ms", "prepare_ms", "sweep_ms", "level0_sweep_ms",
                                                "icm_ms", "energy_ms", "download_ms")] + \
                [(n, ctypes.c_int64) for n in ("kernel_launches", "level0_sweep_launches", "node_label_iters",
-                                              "h2d_bytes", "d2h_bytes")]
+                                              "h2d_bytes", "d2h_bytes", "warm_start_used")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -89,9 +89,30 @@ def lib():
         L.ginf_batch_destroy.argtypes = [_p]
         L.ginf_decode_bp_batch.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(_p), _i32, _i32,
                                            ctypes.POINTER(Options), ctypes.POINTER(Stats)]
+        L.ginf_warmnet_create.argtypes = [ctypes.POINTER(_p), _i32, _i32, ctypes.c_uint64]
+        L.ginf_warmnet_load.argtypes = [ctypes.POINTER(_p), ctypes.c_char_p]
+        L.ginf_warmnet_save.argtypes = [_p, ctypes.c_char_p]
+        L.ginf_warmnet_destroy.argtypes = [_p]
+        L.ginf_warmnet_num_params.argtypes = [_p, ctypes.POINTER(ctypes.c_int64)]
+        L.ginf_warmnet_get_params.argtypes = [_p, _p]
+        L.ginf_warmnet_set_params.argtypes = [_p, _p]
+        L.ginf_warmnet_forward.argtypes = [_p, _p, _i32, _i32, _i32, _p, _p]
+        L.ginf_warmnet_gradients.argtypes = [_p, _p, _p, _i32, _i32, _i32, ctypes.POINTER(ctypes.c_float), _p, _p]
+        L.ginf_warmnet_train_step.argtypes = [_p, _p, _p, _i32, _i32, _i32, ctypes.c_float,
+                                              ctypes.POINTER(ctypes.c_float), _p]
+        L.ginf_hbp_level_state.argtypes = [_p, ctypes.POINTER(Grid), _i32, _i32, _i32, _i32, _p, _p,
+                                           ctypes.POINTER(Options)]
+        L.ginf_decode_hbp_learned.argtypes = [_p, ctypes.POINTER(Grid), _i32, _i32, _i32, _i32, _i32, _p, _p,
+                                              ctypes.POINTER(Options), ctypes.POINTER(Stats)]
+        L.ginf_decode_hbp_warm.argtypes = [_p, ctypes.POINTER(Grid), _i32, _i32, _i32, _i32, _i32, _p, _i32, _p,
+                                           ctypes.POINTER(Options), ctypes.POINTER(Stats)]
         for name in ("ginf_decode_hbp", "ginf_decode_icm", "ginf_energy", "ginf_solve", "ginf_stereo_costs",
                      "ginf_workspace_create", "ginf_workspace_destroy", "ginf_batch_create", "ginf_batch_run",
-                     "ginf_batch_config", "ginf_batch_destroy", "ginf_decode_bp_batch"):
+                     "ginf_batch_config", "ginf_batch_destroy", "ginf_decode_bp_batch", "ginf_warmnet_create",
+                     "ginf_warmnet_load", "ginf_warmnet_save", "ginf_warmnet_destroy", "ginf_warmnet_num_params",
+                     "ginf_warmnet_get_params", "ginf_warmnet_set_params", "ginf_warmnet_forward",
+                     "ginf_warmnet_gradients", "ginf_warmnet_train_step", "ginf_hbp_level_state",
+                     "ginf_decode_hbp_learned", "ginf_decode_hbp_warm"):
             getattr(L, name).restype = _i32
         _lib = L
     return _lib
@@ -297,6 +318,134 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class WarmNet:
+    """The warm-start network (``ginf_warmnet``).  Tensors are CUDA FP32,
+    shaped (n, h, w, L)."""
+
+    def __init__(self, num_labels=64, hidden=32, seed=0, path=None):
+        h = _p()
+        if path is not None:
+            check(lib().ginf_warmnet_load(ctypes.byref(h), str(path).encode()))
+        else:
+            check(lib().ginf_warmnet_create(ctypes.byref(h), num_labels, hidden, seed))
+        self.handle = h
+
+    def num_params(self):
+        n = ctypes.c_int64()
+        check(lib().ginf_warmnet_num_params(self.handle, ctypes.byref(n)))
+        return n.value
+
+    def get_params(self):
+        out = np.zeros(self.num_params(), np.float32)
+        check(lib().ginf_warmnet_get_params(self.handle, out.ctypes.data))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        check(lib().ginf_warmnet_set_params(self.handle, p.ctypes.data))
+
+    def forward(self, x, stream=None):
+        import torch
+        n, h, w, _ = x.shape
+        y = torch.empty_like(x)
+        check(lib().ginf_warmnet_forward(self.handle, x.data_ptr(), n, h, w, y.data_ptr(), stream))
+        return y
+
+    def gradients(self, x, target, stream=None):
+        n, h, w, _ = x.shape
+        loss = ctypes.c_float()
+        g = np.zeros(self.num_params(), np.float32)
+        check(lib().ginf_warmnet_gradients(self.handle, x.data_ptr(), target.data_ptr(), n, h, w, ctypes.byref(loss),
+                                           g.ctypes.data, stream))
+        return loss.value, g
+
+    def train_step(self, x, target, lr, stream=None):
+        n, h, w, _ = x.shape
+        loss = ctypes.c_float()
+        check(lib().ginf_warmnet_train_step(self.handle, x.data_ptr(), target.data_ptr(), n, h, w, lr,
+                                            ctypes.byref(loss), stream))
+        return loss.value
+
+    def save(self, path):
+        check(lib().ginf_warmnet_save(self.handle, str(path).encode()))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().ginf_warmnet_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def level_state(D, V, model, levels, iters, level, want_beliefs=True, target=0, workspace=None, **opt):
+    """(x, target) of pyramid level `level` as CUDA FP32 (H_t, W_t, L); target
+    0 = the level's own beliefs, 1 = projected finest-level messages."""
+    import torch
+    L, H, W = D.shape
+    Wt, Ht = W, H
+    for _ in range(level):
+        Wt, Ht = (Wt + 1) // 2, (Ht + 1) // 2
+    x = torch.empty((Ht, Wt, L), dtype=torch.float32, device=D.device)
+    b = torch.empty_like(x) if want_beliefs else None
+    g = make_grid(D, V, model)
+    o = options(**opt)
+    ws = workspace.handle if workspace is not None else None
+    check(lib().ginf_hbp_level_state(ws, ctypes.byref(g), levels, iters, level, target, x.data_ptr(),
+                                     b.data_ptr() if b is not None else None, ctypes.byref(o)))
+    return x, b
+
+
+def decode_hbp_learned(D, V, model, levels, iters, warm_level, net, labels=None, *, warm_iters=None, mid_iters=-1,
+                       workspace=None, want_stats=False, **opt):
+    """Hierarchical BP with level `warm_level` seeded by the network `net`
+    (warm_iters half-sweeps there, default `iters`; mid_iters at the levels
+    between it and level 0, default `iters`) and the cold fallback."""
+    L, H, W = D.shape
+    g = make_grid(D, V, model)
+    lab = labels if labels is not None else _new_like(D, (H, W), np.int32)
+    o = options(**opt)
+    st = Stats()
+    ws = workspace.handle if workspace is not None else None
+    wi = iters if warm_iters is None else warm_iters
+    check(lib().ginf_decode_hbp_learned(ws, ctypes.byref(g), levels, iters, warm_level, wi, mid_iters, net.handle,
+                                        _ptr(lab)[0], ctypes.byref(o), ctypes.byref(st) if want_stats else None))
+    return (lab, st.as_dict()) if want_stats else lab
+
+
+def decode_hbp_warm(D, V, model, levels, iters, warm_level, prediction, labels=None, *, warm_iters=None,
+                    mid_iters=-1, fallback=True, workspace=None, want_stats=False, **opt):
+    """Hierarchical BP with level `warm_level` seeded from `prediction`, a CUDA
+    FP32 tensor (H_t, W_t, L) on the warm-start network's output scale."""
+    import torch
+    L, H, W = D.shape
+    g = make_grid(D, V, model)
+    lab = labels if labels is not None else _new_like(D, (H, W), np.int32)
+    o = options(**opt)
+    st = Stats()
+    ws = workspace.handle if workspace is not None else None
+    wi = iters if warm_iters is None else warm_iters
+    Wt, Ht = W, H
+    for _ in range(warm_level):
+        Wt, Ht = (Wt + 1) // 2, (Ht + 1) // 2
+    if tuple(prediction.shape) != (Ht, Wt, L) or prediction.dtype != torch.float32 or not prediction.is_cuda:
+        raise ValueError(f"prediction must be a CUDA float32 tensor of shape {(Ht, Wt, L)}")
+    pred = prediction.contiguous()
+    check(lib().ginf_decode_hbp_warm(ws, ctypes.byref(g), levels, iters, warm_level, wi, mid_iters, pred.data_ptr(),
+                                     1 if fallback else 0, _ptr(lab)[0], ctypes.byref(o),
+                                     ctypes.byref(st) if want_stats else None))
+    return (lab, st.as_dict()) if want_stats else lab
 
 
 def version() -> str:

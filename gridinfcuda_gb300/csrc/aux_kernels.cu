@@ -352,6 +352,115 @@ __global__ void k_stereo_costs(int W, int H, int L, const float *__restrict__ le
     costs[idx] = coef * fminf(fabsf(a - b), cap);
 }
 
+// Level-t inputs and targets of the warm-start network (FP32 records):
+// costs and beliefs per fine node, i.e. divided by scale = 4^t.
+__global__ void k_level_x(const unsigned char *__restrict__ rec, int W, int H, int L, uint32_t rec_bytes, float scale,
+                          float *__restrict__ out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)W * H * L) return;
+    const size_t node = i / L;
+    const int l = (int)(i - node * L);
+    out[i] = reinterpret_cast<const float *>(rec + node * rec_bytes)[l] / scale;
+}
+
+__global__ void k_level_beliefs(const unsigned char *__restrict__ rec, int W, int H, int L, uint32_t rec_bytes,
+                                uint32_t d_bytes, uint32_t m_bytes, float scale, float *__restrict__ out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)W * H * L) return;
+    const size_t node = i / L;
+    const int l = (int)(i - node * L);
+    const int x = (int)(node % W), y = (int)(node / W);
+    const unsigned char *r = rec + node * rec_bytes;
+    float v = reinterpret_cast<const float *>(r)[l];
+    for (int d = 0; d < 4; ++d) {
+        const int qx = x + ddx(d), qy = y + ddy(d);
+        if (qx < 0 || qy < 0 || qx >= W || qy >= H || on_border(qx, qy, W, H)) continue;
+        v += reinterpret_cast<const float *>(r + d_bytes + d * m_bytes)[l];
+    }
+    out[i] = v / scale;
+}
+
+// Fine-level target of the warm start: for each node of level t, its costs
+// plus the mean over its fine block (2^t x 2^t level-0 nodes, clipped at the
+// grid edge) of the level-0 incoming-message sums, divided by 4^t.
+__global__ void k_project_fine(const unsigned char *__restrict__ rec0, int W0, int H0,
+                               const unsigned char *__restrict__ rect, int Wt, int Ht, int t, int L,
+                               uint32_t rec_bytes, uint32_t d_bytes, uint32_t m_bytes, float *__restrict__ out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)Wt * Ht * L) return;
+    const size_t node = i / L;
+    const int l = (int)(i - node * L);
+    const int X = (int)(node % Wt), Y = (int)(node / Wt);
+    const int bs = 1 << t;
+    float sum = 0.f;
+    int count = 0;
+    for (int y = Y * bs; y < min(H0, (Y + 1) * bs); ++y)
+        for (int x = X * bs; x < min(W0, (X + 1) * bs); ++x) {
+            const unsigned char *r = rec0 + ((size_t)y * W0 + x) * rec_bytes + d_bytes;
+            for (int d = 0; d < 4; ++d) {
+                const int qx = x + ddx(d), qy = y + ddy(d);
+                if (qx < 0 || qy < 0 || qx >= W0 || qy >= H0 || on_border(qx, qy, W0, H0)) continue;
+                sum += reinterpret_cast<const float *>(r + d * m_bytes)[l];
+            }
+            ++count;
+        }
+    const float D = reinterpret_cast<const float *>(rect + node * rec_bytes)[l];
+    out[i] = (D + sum / (float)max(count, 1)) / (float)(bs * bs);
+}
+
+// Labelling that level t hands to the fine level: per node the lowest label
+// minimising D_t / 4^t + (sum of incoming messages), i.e. the block mean of
+// the beliefs the level-0 nodes start from after the coarse-to-fine copies.
+// One warp per node, labels strided over the lanes, FP32 native records.
+__global__ void k_level_labels_fine(const unsigned char *__restrict__ rec, int W, int H, int L, uint32_t rec_bytes,
+                                    uint32_t d_bytes, uint32_t m_bytes, float inv_scale, int32_t *__restrict__ lab) {
+    const size_t node = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (node >= (size_t)W * H) return;
+    const int x = (int)(node % W), y = (int)(node / W);
+    const unsigned char *r = rec + node * rec_bytes;
+    float best = INFINITY;
+    int arg = 0x7fffffff;
+    for (int l = lane; l < L; l += 32) {
+        float v = reinterpret_cast<const float *>(r)[l] * inv_scale;
+        for (int d = 0; d < 4; ++d) {
+            const int qx = x + ddx(d), qy = y + ddy(d);
+            if (qx < 0 || qy < 0 || qx >= W || qy >= H || on_border(qx, qy, W, H)) continue;
+            v += reinterpret_cast<const float *>(r + d_bytes + d * m_bytes)[l];
+        }
+        if (v < best) { best = v; arg = l; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oa = __shfl_xor_sync(0xffffffffu, arg, o);
+        if (ob < best || (ob == best && oa < arg)) { best = ob; arg = oa; }
+    }
+    if (lane == 0) lab[node] = arg == 0x7fffffff ? 0 : arg;
+}
+
+// Level-0 labelling that gives every node its level-t block's label.
+__global__ void k_upsample_labels(const int32_t *__restrict__ lab_t, int Wt, int t, int32_t *__restrict__ lab0,
+                                  int W0, int H0) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)W0 * H0) return;
+    const int x = (int)(i % W0), y = (int)(i / W0);
+    lab0[i] = lab_t[(size_t)(y >> t) * Wt + (x >> t)];
+}
+
+// Warm start: every incoming slot of every node of level t holds
+// factor * (y - x), a quarter of the predicted message sum (factor = 4^t / 4).
+__global__ void k_warm_init(unsigned char *__restrict__ rec, int W, int H, int L, int Lp, uint32_t rec_bytes,
+                            uint32_t d_bytes, uint32_t m_bytes, const float *__restrict__ y,
+                            const float *__restrict__ x, float factor) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)W * H * Lp) return;
+    const size_t node = i / Lp;
+    const int l = (int)(i - node * Lp);
+    const float v = l < L ? factor * (y[node * L + l] - x[node * L + l]) : 0.f;
+    unsigned char *r = rec + node * rec_bytes + d_bytes;
+    for (int d = 0; d < 4; ++d) reinterpret_cast<float *>(r + d * m_bytes)[l] = v;
+}
+
 }  // namespace
 
 RecordFormat make_format(int ctype, int store, int L) {
@@ -539,6 +648,46 @@ cudaError_t launch_convert_table(int src_type, int dst_type, const void *src, vo
         k_convert<float, int><<<b, kThreads, 0, s>>>(static_cast<const float *>(src), static_cast<int *>(dst), n);
     else
         return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_level_x(const RecordFormat &f, const unsigned char *rec, int W, int H, float scale, float *out,
+                           cudaStream_t s) {
+    if (f.ctype != CT_F32) return cudaErrorInvalidValue;
+    k_level_x<<<blocks_for((size_t)W * H * f.L), kThreads, 0, s>>>(rec, W, H, f.L, f.rec_bytes, scale, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_level_beliefs(const RecordFormat &f, const unsigned char *rec, int W, int H, float scale,
+                                 float *out, cudaStream_t s) {
+    if (f.ctype != CT_F32 || f.store != ST_NATIVE) return cudaErrorInvalidValue;
+    k_level_beliefs<<<blocks_for((size_t)W * H * f.L), kThreads, 0, s>>>(rec, W, H, f.L, f.rec_bytes, f.d_bytes,
+                                                                         f.m_bytes, scale, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fine_labels(const RecordFormat &f, const unsigned char *rect, int Wt, int Ht, int t,
+                               int32_t *lab_t, int32_t *lab0, int W0, int H0, cudaStream_t s) {
+    if (f.ctype != CT_F32 || f.store != ST_NATIVE) return cudaErrorInvalidValue;
+    k_level_labels_fine<<<blocks_for((size_t)Wt * Ht * 32), kThreads, 0, s>>>(
+        rect, Wt, Ht, f.L, f.rec_bytes, f.d_bytes, f.m_bytes, 1.f / (float)(1u << (2 * t)), lab_t);
+    k_upsample_labels<<<blocks_for((size_t)W0 * H0), kThreads, 0, s>>>(lab_t, Wt, t, lab0, W0, H0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_project_fine(const RecordFormat &f, const unsigned char *rec0, int W0, int H0,
+                                const unsigned char *rect, int Wt, int Ht, int t, float *out, cudaStream_t s) {
+    if (f.ctype != CT_F32 || f.store != ST_NATIVE) return cudaErrorInvalidValue;
+    k_project_fine<<<blocks_for((size_t)Wt * Ht * f.L), kThreads, 0, s>>>(rec0, W0, H0, rect, Wt, Ht, t, f.L,
+                                                                          f.rec_bytes, f.d_bytes, f.m_bytes, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_warm_init(const RecordFormat &f, unsigned char *rec, int W, int H, const float *y, const float *x,
+                             float factor, cudaStream_t s) {
+    if (f.ctype != CT_F32 || f.store != ST_NATIVE) return cudaErrorInvalidValue;
+    k_warm_init<<<blocks_for((size_t)W * H * f.Lp), kThreads, 0, s>>>(rec, W, H, f.L, f.Lp, f.rec_bytes, f.d_bytes,
+                                                                       f.m_bytes, y, x, factor);
     return cudaGetLastError();
 }
 

@@ -20,6 +20,9 @@
 using namespace ginf_gpu;
 
 namespace ginf_gpu {
+ginf_status warmnet_forward(ginf_warmnet *n, const float *x, int nimg, int h, int w, float **y_out, cudaStream_t s);
+int warmnet_labels(const ginf_warmnet *n);
+
 template <typename T, typename M>
 cudaError_t launch_sweep_tm(const RecordFormat &, const SweepConfig &, const SweepParams &, cudaStream_t, int);
 
@@ -376,8 +379,11 @@ ginf_status table_radius(Call &c, Prepared &P, int &radius) {
     return GINF_OK;
 }
 
-// The HBP level loop on prepared records: bp.cc:121-166 (bp.cu:180-205).
-ginf_status run_bp(Call &c, Prepared &P, int iters, int64_t &nli) {
+// The HBP level loop on prepared records, levels `from` down to `to`:
+// bp.cc:121-166 (bp.cu:180-205).  Level `from` starts from zero messages at
+// the top of the pyramid, from the coarser level otherwise, or from the
+// messages already in its records when top_initialised.
+ginf_status run_levels(Call &c, Prepared &P, int iters, int64_t &nli, int from, int to, bool top_initialised) {
     const RecordFormat &f = P.f;
     cudaStream_t s = c.r.stream;
     int radius = 9;
@@ -386,12 +392,11 @@ ginf_status run_bp(Call &c, Prepared &P, int iters, int64_t &nli) {
     const bool stale = c.r.decode == GINF_DECODE_STALE;
     const int W0 = P.lv[0].W, H0 = P.lv[0].H;
     // Nodes a level-0 colour never updates keep the argmin of a zero belief.
-    if (stale && iters < 2 && W0 >= 3 && H0 >= 3) {
+    if (to == 0 && stale && iters < 2 && W0 >= 3 && H0 >= 3) {
         GINF_CK(launch_fill_interior(P.lab, W0, H0, 0, s));
         ++c.launches;
     }
-    nli = 0;
-    for (int t = T - 1; t >= 0; --t) {
+    for (int t = from; t >= to; --t) {
         const Level &lv = P.lv[t];
         unsigned char *rec = P.rec + lv.off;
         const bool interior = lv.W >= 3 && lv.H >= 3;
@@ -400,7 +405,9 @@ ginf_status run_bp(Call &c, Prepared &P, int iters, int64_t &nli) {
         // (or as zeros at the top) and no initialisation pass is needed.
         const bool fused = iters >= 2 && interior;
         int first = RD_OWN;
-        if (t == T - 1) {
+        if (t == from && top_initialised) {
+            first = RD_OWN;
+        } else if (t == T - 1) {
             if (fused) first = RD_ZERO;
             else {
                 GINF_CK(launch_init_messages(f, rec, lv.W, lv.H, nullptr, 0, 0, s));
@@ -450,12 +457,19 @@ ginf_status run_bp(Call &c, Prepared &P, int iters, int64_t &nli) {
         }
         nli += (int64_t)lv.W * lv.H * f.L * iters;
     }
-    if (!stale && W0 >= 3 && H0 >= 3) {
-        GINF_CK(launch_decode_fresh(f, P.rec, W0, H0, P.lab, s));
-        ++c.launches;
+    if (to == 0) {
+        if (!stale && W0 >= 3 && H0 >= 3) {
+            GINF_CK(launch_decode_fresh(f, P.rec, W0, H0, P.lab, s));
+            ++c.launches;
+        }
+        c.ev(EV_SWEEPS);
     }
-    c.ev(EV_SWEEPS);
     return GINF_OK;
+}
+
+ginf_status run_bp(Call &c, Prepared &P, int iters, int64_t &nli) {
+    nli = 0;
+    return run_levels(c, P, iters, nli, (int)P.lv.size() - 1, 0, false);
 }
 
 // Jacobi ICM (icm.cc:4-38) from P.lab, result in P.lab.
@@ -768,6 +782,197 @@ ginf_status ginf_solve(ginf_workspace *wsp, const ginf_grid *grid, int32_t num_l
     GINF_TRY(read_status(c, P));
     if (energy) *energy = *c.ws->energy_host;
     return finish(c, nli);
+}
+
+// The learned warm start needs FP32 arithmetic, the native store and the
+// truncated-linear / Potts update.
+ginf_status check_learned(const ginf_grid *grid, const Resolved &r) {
+    if (r.ctype != GINF_F32 || r.store != ST_NATIVE || r.mode != MODE_LINEAR)
+        return fail(GINF_ERR_UNSUPPORTED, "the warm start runs FP32 BP with Potts / truncated-linear smoothness");
+    if (grid->memory != GINF_DEVICE) return fail(GINF_ERR_INVALID_ARGUMENT, "the warm start takes device buffers");
+    return GINF_OK;
+}
+
+ginf_status ginf_hbp_level_state(ginf_workspace *wsp, const ginf_grid *grid, int32_t num_levels,
+                                 int32_t iters_per_level, int32_t level, int32_t target, float *x_out,
+                                 float *beliefs_out, const ginf_options *opt) {
+    g_last_error.clear();
+    GINF_TRY(check_grid(grid));
+    if (num_levels < 1 || level < 0 || level >= num_levels || iters_per_level < 0)
+        return fail(GINF_ERR_INVALID_ARGUMENT, "need 0 <= level < num_levels and iters_per_level >= 0");
+    Call c;
+    GINF_TRY(resolve(grid, opt, c.r));
+    GINF_TRY(check_learned(grid, c.r));
+    if (grid->num_labels > kMaxLabels) return fail(GINF_ERR_UNSUPPORTED, "too many labels");
+    WsGuard guard(wsp);
+    c.ws = guard.ws;
+    c.g = grid;
+    c.stats = nullptr;
+    GINF_TRY(ws_init(c.ws));
+    Prepared P;
+    GINF_TRY(prepare(c, P, num_levels, false, nullptr, nullptr));
+    const Level &lt = P.lv[level];
+    const float scale = (float)(1u << (2 * level));
+    if (x_out) GINF_CK(launch_level_x(P.f, P.rec + lt.off, lt.W, lt.H, scale, x_out, c.r.stream));
+    if (beliefs_out) {
+        int64_t nli = 0;
+        if (target == 1) {
+            // the whole schedule, then the level-0 message sums averaged per block
+            GINF_TRY(run_levels(c, P, iters_per_level, nli, num_levels - 1, 0, false));
+            GINF_CK(launch_project_fine(P.f, P.rec, P.lv[0].W, P.lv[0].H, P.rec + lt.off, lt.W, lt.H, level,
+                                        beliefs_out, c.r.stream));
+        } else {
+            GINF_TRY(run_levels(c, P, iters_per_level, nli, num_levels - 1, level, false));
+            GINF_CK(launch_level_beliefs(P.f, P.rec + lt.off, lt.W, lt.H, scale, beliefs_out, c.r.stream));
+        }
+    }
+    GINF_TRY(read_status(c, P));
+    return GINF_OK;
+}
+
+// Level-0 energy of the labelling level t hands down (each level-0 node
+// takes its block's argmin of D_t / 4^t + incoming messages); into dst
+// (device double).
+ginf_status handed_down_energy(Call &c, Prepared &P, int t, int32_t *lab_t, int32_t *lab0, double *partials, int np,
+                               double *dst) {
+    const Level &lt = P.lv[t];
+    const Level &l0 = P.lv[0];
+    cudaStream_t s = c.r.stream;
+    GINF_CK(launch_fine_labels(P.f, P.rec + lt.off, lt.W, lt.H, t, lab_t, lab0, l0.W, l0.H, s));
+    GINF_CK(launch_energy(P.f.ctype, P.rec, P.f.rec_bytes / P.f.t_size, 1, l0.W, l0.H, P.f.L, P.Vt, lab0, partials,
+                          np, dst, P.status, s));
+    c.launches += 4;
+    return GINF_OK;
+}
+
+}  // extern "C"
+
+// Hierarchical BP with level t seeded from a prediction: by the network when
+// net is given (pred is then NULL), else from the caller's device buffer pred
+// ([H_t][W_t][L], the network's output scale).
+static ginf_status decode_hbp_seeded(ginf_workspace *wsp, const ginf_grid *grid, int32_t num_levels,
+                                     int32_t iters_per_level, int32_t warm_level, int32_t warm_iters,
+                                     int32_t mid_iters, ginf_warmnet *net, const float *pred, int32_t fallback,
+                                     int32_t *labels, const ginf_options *opt, ginf_stats *stats) {
+    g_last_error.clear();
+    GINF_TRY(check_grid(grid));
+    if ((!net && !pred) || !labels) return fail(GINF_ERR_INVALID_ARGUMENT, "prediction / labels is NULL");
+    if (num_levels < 2 || warm_level < 1 || warm_level >= num_levels || iters_per_level < 0 || warm_iters < 0)
+        return fail(GINF_ERR_INVALID_ARGUMENT, "need 1 <= warm_level < num_levels and iteration counts >= 0");
+    if (net && warmnet_labels(net) != grid->num_labels)
+        return fail(GINF_ERR_INVALID_ARGUMENT, "the network was built for another label count");
+    Call c;
+    GINF_TRY(resolve(grid, opt, c.r));
+    GINF_TRY(check_learned(grid, c.r));
+    WsGuard guard(wsp);
+    c.ws = guard.ws;
+    c.g = grid;
+    c.stats = stats;
+    GINF_TRY(ws_init(c.ws));
+    begin(c);
+    Prepared P;
+    GINF_TRY(prepare(c, P, num_levels, false, nullptr, labels));
+    cudaStream_t s = c.r.stream;
+    const int t = warm_level;
+    const int sl = t + 1;  // the cold screening level
+    if (fallback && sl > num_levels - 1)
+        return fail(GINF_ERR_INVALID_ARGUMENT, "the fallback needs a pyramid level above warm_level");
+    const Level &lt = P.lv[t];
+    const Level &l0 = P.lv[0];
+    const size_t nx = (size_t)lt.W * lt.H * P.f.L;
+    const int np = energy_num_partials(l0.W, l0.H);
+    const size_t lab_s_bytes = fallback ? align_up((size_t)P.lv[sl].W * P.lv[sl].H * sizeof(int32_t), 256) : 0;
+    const size_t lab0_bytes = fallback ? align_up((size_t)l0.W * l0.H * sizeof(int32_t), 256) : 0;
+    unsigned char *scratch = nullptr;
+    const size_t scratch_bytes = align_up(nx * sizeof(float), 256) + lab_s_bytes + lab0_bytes + sizeof(double) * (np + 2);
+    GINF_CK(cudaMallocAsync(reinterpret_cast<void **>(&scratch), scratch_bytes, s));
+    float *x = reinterpret_cast<float *>(scratch);
+    int32_t *lab_s = reinterpret_cast<int32_t *>(scratch + align_up(nx * sizeof(float), 256));
+    int32_t *lab0 = reinterpret_cast<int32_t *>(reinterpret_cast<unsigned char *>(lab_s) + lab_s_bytes);
+    double *partials = reinterpret_cast<double *>(reinterpret_cast<unsigned char *>(lab0) + lab0_bytes);
+    double *energies = partials + np;  // [cold screen, warm result]
+    ginf_status st = GINF_OK;
+    int64_t nli = 0;
+    float *y = const_cast<float *>(pred);
+    double e_host[2] = {0.0, 0.0};
+    const float scale = (float)(1u << (2 * t));
+    bool warm = true;
+    if (mid_iters < 0) mid_iters = iters_per_level;
+    do {
+        cudaError_t e;
+        if (fallback) {
+            // Cold schedule down to the level above the seeded one (cheap):
+            // its handed-down labelling is the bar the seeded result must meet,
+            // and its state is where the cold fallback resumes.
+            if ((st = run_levels(c, P, iters_per_level, nli, num_levels - 1, sl, false)) != GINF_OK) break;
+            if ((st = handed_down_energy(c, P, sl, lab_s, lab0, partials, np, energies)) != GINF_OK) break;
+        }
+        // Network input and prediction at level t.
+        if ((e = launch_level_x(P.f, P.rec + lt.off, lt.W, lt.H, scale, x, s)) != cudaSuccess) {
+            st = cuda_fail(e, "level costs");
+            break;
+        }
+        ++c.launches;
+        if (net) {
+            if ((st = warmnet_forward(net, x, 1, lt.H, lt.W, &y, s)) != GINF_OK) break;
+            c.launches += 5;
+        }
+        // Seeded path: level-t messages from the prediction, its own sweeps,
+        // then the finer levels.
+        if ((e = launch_warm_init(P.f, P.rec + lt.off, lt.W, lt.H, y, x, scale / 4.f, s)) != cudaSuccess) {
+            st = cuda_fail(e, "warm init");
+            break;
+        }
+        ++c.launches;
+        if (warm_iters > 0 && (st = run_levels(c, P, warm_iters, nli, t, t, true)) != GINF_OK) break;
+        if (t > 1 && (st = run_levels(c, P, mid_iters, nli, t - 1, 1, false)) != GINF_OK) break;
+        if ((st = run_levels(c, P, iters_per_level, nli, 0, 0, false)) != GINF_OK) break;
+        if (fallback) {
+            if ((e = launch_energy(P.f.ctype, P.rec, P.f.rec_bytes / P.f.t_size, 1, l0.W, l0.H, P.f.L, P.Vt, P.lab,
+                                   partials, np, energies + 1, P.status, s)) != cudaSuccess ||
+                (e = cudaMemcpyAsync(e_host, energies, 2 * sizeof(double), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+                (e = cudaStreamSynchronize(s)) != cudaSuccess) {
+                st = cuda_fail(e, "seeded energy");
+                break;
+            }
+            c.launches += 2;
+            // A seeded result above the cold coarse labelling's energy is
+            // discarded: the cold schedule resumes below the screening level,
+            // which gives exactly the plain hierarchical result.
+            warm = e_host[1] <= e_host[0];
+            if (!warm && (st = run_levels(c, P, iters_per_level, nli, sl - 1, 0, false)) != GINF_OK) break;
+        }
+    } while (false);
+    cudaFreeAsync(scratch, s);
+    if (st != GINF_OK) return st;
+    c.ev(EV_ICM);
+    c.ev(EV_ENERGY);
+    GINF_TRY(labels_to_caller(c, P, labels, true));
+    c.ev(EV_END);
+    GINF_TRY(read_status(c, P));
+    st = finish(c, nli);
+    if (stats) stats->warm_start_used = warm ? 1 : 0;
+    return st;
+}
+
+extern "C" {
+
+ginf_status ginf_decode_hbp_learned(ginf_workspace *wsp, const ginf_grid *grid, int32_t num_levels,
+                                    int32_t iters_per_level, int32_t warm_level, int32_t warm_iters,
+                                    int32_t mid_iters, ginf_warmnet *net, int32_t *labels, const ginf_options *opt,
+                                    ginf_stats *stats) {
+    if (!net) return fail(GINF_ERR_INVALID_ARGUMENT, "net is NULL");
+    return decode_hbp_seeded(wsp, grid, num_levels, iters_per_level, warm_level, warm_iters, mid_iters, net, nullptr,
+                             1, labels, opt, stats);
+}
+
+ginf_status ginf_decode_hbp_warm(ginf_workspace *wsp, const ginf_grid *grid, int32_t num_levels,
+                                 int32_t iters_per_level, int32_t warm_level, int32_t warm_iters, int32_t mid_iters,
+                                 const float *prediction, int32_t fallback, int32_t *labels, const ginf_options *opt,
+                                 ginf_stats *stats) {
+    if (!prediction) return fail(GINF_ERR_INVALID_ARGUMENT, "prediction is NULL");
+    return decode_hbp_seeded(wsp, grid, num_levels, iters_per_level, warm_level, warm_iters, mid_iters, nullptr,
+                             prediction, fallback, labels, opt, stats);
 }
 
 ginf_status ginf_stereo_costs(int32_t width, int32_t height, int32_t num_labels, int32_t memory, const float *left,

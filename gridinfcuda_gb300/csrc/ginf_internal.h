@@ -102,6 +102,18 @@ cudaError_t launch_energy(int ctype, const void *costs, size_t node_stride, size
                           int *status, cudaStream_t s);
 int energy_num_partials(int W, int H);
 cudaError_t launch_convert_table(int src_type, int dst_type, const void *src, void *dst, int n, cudaStream_t s);
+// Warm-start helpers (FP32 records, native store).
+cudaError_t launch_level_x(const RecordFormat &f, const unsigned char *rec, int W, int H, float scale, float *out,
+                           cudaStream_t s);
+cudaError_t launch_level_beliefs(const RecordFormat &f, const unsigned char *rec, int W, int H, float scale,
+                                 float *out, cudaStream_t s);
+cudaError_t launch_fine_labels(const RecordFormat &f, const unsigned char *rect, int Wt, int Ht, int t,
+                               int32_t *lab_t, int32_t *lab0, int W0, int H0, cudaStream_t s);
+cudaError_t launch_project_fine(const RecordFormat &f, const unsigned char *rec0, int W0, int H0,
+                                const unsigned char *rect, int Wt, int Ht, int t, float *out, cudaStream_t s);
+cudaError_t launch_warm_init(const RecordFormat &f, unsigned char *rec, int W, int H, const float *y, const float *x,
+                             float factor, cudaStream_t s);
+
 // Sets the message ginf_last_error() returns on this host thread.
 void set_last_error(const char *msg);
 

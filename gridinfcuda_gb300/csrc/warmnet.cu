@@ -1,0 +1,746 @@
+// warmnet.cu -- the learned warm start: a small convolutional network that
+// maps the costs of a coarse pyramid level to that level's BP beliefs, with
+// hand-written tensor-core (mma.sync m16n8k16 BF16, FP32 accumulate)
+// forward, data-gradient and weight-gradient kernels, the loss, ReLU,
+// bias-gradient and Adam kernels, and a checkpoint format.
+//
+// Network (L labels, h hidden channels): conv3x3(L->h) ReLU, conv3x3(h->h)
+// ReLU, conv3x3(h->h) ReLU, conv3x3(h->L); zero padding; activations NHWC.
+// Input x = D_t / 4^t (the level's costs per fine node), output
+// y = x + net(x), trained towards the beliefs B_t / 4^t of a long
+// hierarchical BP run.  Rounding points (mirrored by oracle/warmnet_ref.py):
+// x, weights and hidden activations in BF16; sums in FP32; the output and
+// every gradient in FP32, rounded to BF16 where they feed a tensor-core
+// product.  The reference has no learned component: this whole file is new.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ginf_gb300.h"
+#include "ginf_internal.h"
+
+namespace ginf_gpu {
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned nblocks(size_t n, int per = kThreads) { return (unsigned)((n + per - 1) / per); }
+
+__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+struct Geo {
+    int n, h, w;  // images, rows, columns
+};
+
+// Pair of input channels (c, c+1) at the pixel shifted by (dy, dx), zero
+// outside the image.
+__device__ __forceinline__ uint32_t load_pair(const __nv_bfloat16 *in, int cin, Geo g, int pix, int dy, int dx,
+                                              int c) {
+    const int x = pix % g.w, t = pix / g.w, y = t % g.h, n = t / g.h;
+    const int yy = y + dy, xx = x + dx;
+    if (pix < 0 || yy < 0 || yy >= g.h || xx < 0 || xx >= g.w) return 0u;
+    return *reinterpret_cast<const uint32_t *>(in + ((size_t)(n * g.h + yy) * g.w + xx) * cin + c);
+}
+
+// Forward 3x3 convolution as an implicit GEMM: M = pixels, N = COUT,
+// K = 9*CIN.  A warp owns 16 consecutive pixels and all COUT outputs; each
+// mma consumes one 16-channel slice of one tap.  Weights w[co][tap][ci].
+// RELU applies max(0, .); OUT_F32 writes FP32 (else BF16).  With RES the
+// FP32 output is res + conv (the residual of the last layer).
+template <int CIN, int COUT, bool RELU, bool OUT_F32, bool BIAS>
+__global__ void __launch_bounds__(128) k_conv_fwd(const __nv_bfloat16 *__restrict__ in, const __nv_bfloat16 *__restrict__ w,
+                                                  const float *__restrict__ bias, Geo g, void *out,
+                                                  const float *__restrict__ res) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gid = lane >> 2, tig = lane & 3;
+    const int npix = g.n * g.h * g.w;
+    const int p0 = (blockIdx.x * 4 + warp) * 16;
+    if (p0 >= npix) return;
+    const int pa = p0 + gid, pb = p0 + gid + 8;
+    float acc[COUT / 8][4];
+#pragma unroll
+    for (int j = 0; j < COUT / 8; ++j)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[j][e] = 0.f;
+#pragma unroll 1
+    for (int tap = 0; tap < 9; ++tap) {
+        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+#pragma unroll
+        for (int c0 = 0; c0 < CIN; c0 += 16) {
+            uint32_t a[4];
+            const int c = c0 + tig * 2;
+            a[0] = load_pair(in, CIN, g, pa < npix ? pa : -1, dy, dx, c);
+            a[1] = load_pair(in, CIN, g, pb < npix ? pb : -1, dy, dx, c);
+            a[2] = load_pair(in, CIN, g, pa < npix ? pa : -1, dy, dx, c + 8);
+            a[3] = load_pair(in, CIN, g, pb < npix ? pb : -1, dy, dx, c + 8);
+            const int k = tap * CIN + c;
+#pragma unroll
+            for (int j = 0; j < COUT / 8; ++j) {
+                const __nv_bfloat16 *wr = w + (size_t)(j * 8 + gid) * 9 * CIN + k;
+                uint32_t b[2];
+                b[0] = *reinterpret_cast<const uint32_t *>(wr);
+                b[1] = *reinterpret_cast<const uint32_t *>(wr + 8);
+                mma_bf16(acc[j], a, b);
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < COUT / 8; ++j) {
+        const int co = j * 8 + tig * 2;
+        const float b0 = BIAS ? bias[co] : 0.f, b1 = BIAS ? bias[co + 1] : 0.f;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const int p = half ? pb : pa;
+            if (p >= npix) continue;
+            float v0 = acc[j][2 * half] + b0, v1 = acc[j][2 * half + 1] + b1;
+            if (RELU) {
+                v0 = fmaxf(v0, 0.f);
+                v1 = fmaxf(v1, 0.f);
+            }
+            if (OUT_F32) {
+                if (res) {
+                    v0 += res[(size_t)p * COUT + co];
+                    v1 += res[(size_t)p * COUT + co + 1];
+                }
+                *reinterpret_cast<float2 *>(static_cast<float *>(out) + (size_t)p * COUT + co) = make_float2(v0, v1);
+            } else {
+                *reinterpret_cast<uint32_t *>(static_cast<__nv_bfloat16 *>(out) + (size_t)p * COUT + co) =
+                    pack_bf16(__float2bfloat16_rn(v0), __float2bfloat16_rn(v1));
+            }
+        }
+    }
+}
+
+// Weight gradient: dW[co][tap][ci] = sum over pixels of dout[p][co] *
+// in[p shifted by tap][ci], as GEMM M = COUT, N = 9*CIN, K = pixels.  Block
+// (chunk of kChunk pixels) x (4 warps, one 16x8 output tile each); partial
+// sums per chunk, added in a fixed order by k_reduce_partials.
+constexpr int kChunk = 1024;
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(128) k_conv_wgrad(const __nv_bfloat16 *__restrict__ dout,
+                                                    const __nv_bfloat16 *__restrict__ in, Geo g,
+                                                    float *__restrict__ partials) {
+    constexpr int NT = 9 * CIN / 8;  // n tiles
+    constexpr int TILES = COUT / 16 * NT;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gid = lane >> 2, tig = lane & 3;
+    const int tile = blockIdx.y * 4 + warp;
+    if (tile >= TILES) return;
+    const int mt = tile / NT, nt = tile % NT;
+    const int co_a = mt * 16 + gid, co_b = co_a + 8;
+    const int kcol = nt * 8 + gid;  // this lane's B column
+    const int tap = kcol / CIN, ci = kcol % CIN;
+    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+    const int npix = g.n * g.h * g.w;
+    const int pbeg = blockIdx.x * kChunk, pend = min(npix, pbeg + kChunk);
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    auto dv = [&](int p, int co) -> __nv_bfloat16 {
+        return p < pend ? dout[(size_t)p * COUT + co] : __float2bfloat16_rn(0.f);
+    };
+    auto iv = [&](int p) -> __nv_bfloat16 {
+        if (p >= pend) return __float2bfloat16_rn(0.f);
+        const int x = p % g.w, t = p / g.w, y = t % g.h, n = t / g.h;
+        const int yy = y + dy, xx = x + dx;
+        if (yy < 0 || yy >= g.h || xx < 0 || xx >= g.w) return __float2bfloat16_rn(0.f);
+        return in[((size_t)(n * g.h + yy) * g.w + xx) * CIN + ci];
+    };
+#pragma unroll 1
+    for (int k0 = pbeg; k0 < pend; k0 += 16) {
+        const int q = k0 + tig * 2;
+        uint32_t a[4], b[2];
+        a[0] = pack_bf16(dv(q, co_a), dv(q + 1, co_a));
+        a[1] = pack_bf16(dv(q, co_b), dv(q + 1, co_b));
+        a[2] = pack_bf16(dv(q + 8, co_a), dv(q + 9, co_a));
+        a[3] = pack_bf16(dv(q + 8, co_b), dv(q + 9, co_b));
+        b[0] = pack_bf16(iv(q), iv(q + 1));
+        b[1] = pack_bf16(iv(q + 8), iv(q + 9));
+        mma_bf16(acc, a, b);
+    }
+    // acc: rows co_a / co_b, columns nt*8 + tig*2 + {0,1}
+    float *part = partials + (size_t)blockIdx.x * COUT * 9 * CIN;
+    const int col = nt * 8 + tig * 2;
+    part[(size_t)co_a * 9 * CIN + col] = acc[0];
+    part[(size_t)co_a * 9 * CIN + col + 1] = acc[1];
+    part[(size_t)co_b * 9 * CIN + col] = acc[2];
+    part[(size_t)co_b * 9 * CIN + col + 1] = acc[3];
+}
+
+// Bias gradient partials: sum over a chunk of pixels of g[p][c] (FP32).
+__global__ void k_bias_partials(const float *__restrict__ g, int npix, int C, float *__restrict__ partials) {
+    const int c = threadIdx.x;
+    if (c >= C) return;
+    const int pbeg = blockIdx.x * kChunk, pend = min(npix, pbeg + kChunk);
+    float s = 0.f;
+    for (int p = pbeg; p < pend; ++p) s += g[(size_t)p * C + c];
+    partials[(size_t)blockIdx.x * C + c] = s;
+}
+
+// out[i] = sum over chunks k of partials[k][i], in chunk order.
+__global__ void k_reduce_partials(const float *__restrict__ partials, int chunks, int n, float *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float s = 0.f;
+    for (int k = 0; k < chunks; ++k) s += partials[(size_t)k * n + i];
+    out[i] = s;
+}
+
+// Flipped, transposed weights for the data gradient:
+// wf[ci][tap'][co] = w[co][8 - tap'][ci].
+__global__ void k_flip_weights(const __nv_bfloat16 *__restrict__ w, int cin, int cout, __nv_bfloat16 *__restrict__ wf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cin * 9 * cout) return;
+    const int co = i % cout, tap = (i / cout) % 9, ci = i / (cout * 9);
+    wf[i] = w[((size_t)co * 9 + (8 - tap)) * cin + ci];
+}
+
+__global__ void k_f32_to_bf16(const float *__restrict__ a, __nv_bfloat16 *__restrict__ b, size_t n) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = __float2bfloat16_rn(a[i]);
+}
+
+// Loss = mean((y - t)^2) (per-block double partials), dy = 2 (y - t) / n.
+__global__ void k_mse(const float *__restrict__ y, const float *__restrict__ t, size_t n, float *__restrict__ dy,
+                      double *__restrict__ partials) {
+    double s = 0.0;
+    const float scale = 2.f / (float)n;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float d = y[i] - t[i];
+        s += (double)d * d;
+        dy[i] = scale * d;
+    }
+    __shared__ double red[kThreads];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = kThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partials[blockIdx.x] = red[0];
+}
+
+__global__ void k_sum_double(const double *p, int n, double denom, float *out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double s = 0.0;
+        for (int i = 0; i < n; ++i) s += p[i];
+        *out = (float)(s / denom);
+    }
+}
+
+// g = grad of a ReLU output times (activation > 0), FP32 and a BF16 copy.
+__global__ void k_relu_bwd(const float *__restrict__ grad, const __nv_bfloat16 *__restrict__ act, size_t n,
+                           float *__restrict__ g, __nv_bfloat16 *__restrict__ gb) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float v = __bfloat162float(act[i]) > 0.f ? grad[i] : 0.f;
+    g[i] = v;
+    gb[i] = __float2bfloat16_rn(v);
+}
+
+// Adam (bias-corrected) on FP32 master weights, refreshing the BF16 copy.
+__global__ void k_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m, float *__restrict__ v,
+                       int n, float lr, float b1, float b2, float eps, float c1, float c2,
+                       __nv_bfloat16 *__restrict__ pb) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float upd = lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    const float np = p[i] - upd;
+    p[i] = np;
+    if (pb) pb[i] = __float2bfloat16_rn(np);
+}
+
+uint64_t splitmix(uint64_t &s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+uint64_t fnv1a(const void *data, size_t n, uint64_t h = 1469598103934665603ull) {
+    const unsigned char *p = static_cast<const unsigned char *>(data);
+    for (size_t i = 0; i < n; ++i) {
+        h ^= p[i];
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+}  // namespace
+
+// Conv kernel instantiations for the channel counts the network uses
+// (L in {16, 32, 64}, 32 hidden channels).
+template <int CIN, int COUT, bool RELU, bool OUT_F32>
+cudaError_t conv_fwd_t(const __nv_bfloat16 *in, const __nv_bfloat16 *w, const float *bias, Geo g, void *out,
+                       const float *res, cudaStream_t s) {
+    const int npix = g.n * g.h * g.w;
+    const unsigned blocks = (unsigned)((npix + 63) / 64);
+    if (bias) k_conv_fwd<CIN, COUT, RELU, OUT_F32, true><<<blocks, 128, 0, s>>>(in, w, bias, g, out, res);
+    else k_conv_fwd<CIN, COUT, RELU, OUT_F32, false><<<blocks, 128, 0, s>>>(in, w, bias, g, out, res);
+    return cudaGetLastError();
+}
+
+template <int CIN, int COUT>
+cudaError_t conv_wgrad_t(const __nv_bfloat16 *dout, const __nv_bfloat16 *in, Geo g, float *partials, float *dw,
+                         cudaStream_t s) {
+    const int npix = g.n * g.h * g.w;
+    const int chunks = (npix + kChunk - 1) / kChunk;
+    constexpr int TILES = COUT / 16 * (9 * CIN / 8);
+    k_conv_wgrad<CIN, COUT><<<dim3(chunks, (TILES + 3) / 4), 128, 0, s>>>(dout, in, g, partials);
+    const int n = COUT * 9 * CIN;
+    k_reduce_partials<<<nblocks(n), kThreads, 0, s>>>(partials, chunks, n, dw);
+    return cudaGetLastError();
+}
+
+}  // namespace ginf_gpu
+
+using namespace ginf_gpu;
+
+// ---------------------------------------------------------------------------
+// The network object.
+
+struct ginf_warmnet {
+    int L = 0, hidden = 0;
+    int cin[4], cout[4];
+    size_t woff[4], boff[4], nparams = 0;  // offsets into the flat FP32 parameter vector
+    float *params = nullptr;               // FP32 master weights and biases (device)
+    float *adam_m = nullptr, *adam_v = nullptr;
+    float *grads = nullptr;
+    __nv_bfloat16 *wbf = nullptr;  // BF16 copy of the weights (same offsets)
+    int64_t step = 0;
+    // activations / gradients, grown to the largest batch seen
+    size_t cap_pix = 0;
+    __nv_bfloat16 *a[4] = {};  // a[0] = x (L ch), a[1..3] hidden
+    float *x32 = nullptr;      // residual input (FP32 copy of x)
+    float *y = nullptr;        // output (L ch)
+    float *gy = nullptr;       // dLoss/dy
+    float *g32 = nullptr;      // FP32 gradient scratch (max channels)
+    float *gtmp = nullptr;     // data gradient before the ReLU mask
+    __nv_bfloat16 *gb = nullptr;
+    __nv_bfloat16 *wflip = nullptr;
+    float *partials = nullptr;
+    size_t cap_partials = 0;
+    double *loss_part = nullptr;
+    float *loss_dev = nullptr;
+};
+
+namespace {
+
+ginf_status wfail(ginf_status s, const std::string &m) {
+    ginf_gpu::set_last_error(m.c_str());
+    return s;
+}
+
+#define GINF_WCK(call)                                                                       \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            cudaGetLastError();                                                              \
+            return wfail(GINF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+        }                                                                                    \
+    } while (0)
+
+void layout(ginf_warmnet *n) {
+    const int ch[5] = {n->L, n->hidden, n->hidden, n->hidden, n->L};
+    size_t off = 0;
+    for (int l = 0; l < 4; ++l) {
+        n->cin[l] = ch[l];
+        n->cout[l] = ch[l + 1];
+        n->woff[l] = off;
+        off += (size_t)n->cout[l] * 9 * n->cin[l];
+        n->boff[l] = off;
+        off += n->cout[l];
+    }
+    n->nparams = off;
+}
+
+ginf_status alloc_params(ginf_warmnet *n) {
+    GINF_WCK(cudaMalloc(&n->params, n->nparams * sizeof(float)));
+    GINF_WCK(cudaMalloc(&n->adam_m, n->nparams * sizeof(float)));
+    GINF_WCK(cudaMalloc(&n->adam_v, n->nparams * sizeof(float)));
+    GINF_WCK(cudaMalloc(&n->grads, n->nparams * sizeof(float)));
+    GINF_WCK(cudaMalloc(&n->wbf, n->nparams * sizeof(__nv_bfloat16)));
+    GINF_WCK(cudaMemset(n->adam_m, 0, n->nparams * sizeof(float)));
+    GINF_WCK(cudaMemset(n->adam_v, 0, n->nparams * sizeof(float)));
+    GINF_WCK(cudaMemset(n->grads, 0, n->nparams * sizeof(float)));
+    size_t wf = 0;
+    for (int l = 0; l < 4; ++l) wf = std::max(wf, (size_t)n->cout[l] * 9 * n->cin[l]);
+    GINF_WCK(cudaMalloc(&n->wflip, wf * sizeof(__nv_bfloat16)));
+    GINF_WCK(cudaMalloc(&n->loss_part, 1024 * sizeof(double)));
+    GINF_WCK(cudaMalloc(&n->loss_dev, sizeof(float)));
+    return GINF_OK;
+}
+
+ginf_status refresh_bf16(ginf_warmnet *n, cudaStream_t s) {
+    k_f32_to_bf16<<<nblocks(n->nparams), kThreads, 0, s>>>(n->params, n->wbf, n->nparams);
+    GINF_WCK(cudaGetLastError());
+    return GINF_OK;
+}
+
+ginf_status ensure_batch(ginf_warmnet *n, size_t pix) {
+    if (pix <= n->cap_pix) return GINF_OK;
+    for (int l = 0; l < 4; ++l) cudaFree(n->a[l]);
+    cudaFree(n->x32);
+    cudaFree(n->y);
+    cudaFree(n->gy);
+    cudaFree(n->g32);
+    cudaFree(n->gtmp);
+    cudaFree(n->gb);
+    const size_t cmax = (size_t)std::max(n->L, n->hidden);
+    GINF_WCK(cudaMalloc(&n->a[0], pix * n->L * sizeof(__nv_bfloat16)));
+    for (int l = 1; l < 4; ++l) GINF_WCK(cudaMalloc(&n->a[l], pix * n->hidden * sizeof(__nv_bfloat16)));
+    GINF_WCK(cudaMalloc(&n->x32, pix * n->L * sizeof(float)));
+    GINF_WCK(cudaMalloc(&n->y, pix * n->L * sizeof(float)));
+    GINF_WCK(cudaMalloc(&n->gy, pix * n->L * sizeof(float)));
+    GINF_WCK(cudaMalloc(&n->g32, pix * cmax * sizeof(float)));
+    GINF_WCK(cudaMalloc(&n->gtmp, pix * cmax * sizeof(float)));
+    GINF_WCK(cudaMalloc(&n->gb, pix * cmax * sizeof(__nv_bfloat16)));
+    n->cap_pix = pix;
+    const size_t chunks = (pix + kChunk - 1) / kChunk;
+    size_t need = 0;
+    for (int l = 0; l < 4; ++l) need = std::max(need, chunks * (size_t)n->cout[l] * 9 * n->cin[l]);
+    need = std::max(need, chunks * cmax);
+    if (need > n->cap_partials) {
+        cudaFree(n->partials);
+        GINF_WCK(cudaMalloc(&n->partials, need * sizeof(float)));
+        n->cap_partials = need;
+    }
+    return GINF_OK;
+}
+
+// conv dispatch by (cin, cout) for the supported shapes
+cudaError_t conv_fwd(int cin, int cout, bool relu, bool out_f32, const __nv_bfloat16 *in, const __nv_bfloat16 *w,
+                     const float *bias, Geo g, void *out, const float *res, cudaStream_t s) {
+#define GINF_CONV_CASE(CI, CO)                                                                         \
+    if (cin == CI && cout == CO) {                                                                     \
+        if (out_f32) return conv_fwd_t<CI, CO, false, true>(in, w, bias, g, out, res, s);             \
+        if (relu) return conv_fwd_t<CI, CO, true, false>(in, w, bias, g, out, res, s);                \
+        return conv_fwd_t<CI, CO, false, false>(in, w, bias, g, out, res, s);                         \
+    }
+    GINF_CONV_CASE(16, 32)
+    GINF_CONV_CASE(32, 32)
+    GINF_CONV_CASE(64, 32)
+    GINF_CONV_CASE(32, 16)
+    GINF_CONV_CASE(32, 64)
+#undef GINF_CONV_CASE
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t conv_wgrad(int cin, int cout, const __nv_bfloat16 *dout, const __nv_bfloat16 *in, Geo g, float *part,
+                       float *dw, cudaStream_t s) {
+#define GINF_WG_CASE(CI, CO) \
+    if (cin == CI && cout == CO) return conv_wgrad_t<CI, CO>(dout, in, g, part, dw, s);
+    GINF_WG_CASE(16, 32)
+    GINF_WG_CASE(32, 32)
+    GINF_WG_CASE(64, 32)
+    GINF_WG_CASE(32, 16)
+    GINF_WG_CASE(32, 64)
+#undef GINF_WG_CASE
+    return cudaErrorInvalidValue;
+}
+
+ginf_status forward(ginf_warmnet *n, const float *x, Geo g, cudaStream_t s) {
+    const size_t pix = (size_t)g.n * g.h * g.w;
+    ginf_status st = ensure_batch(n, pix);
+    if (st != GINF_OK) return st;
+    GINF_WCK(cudaMemcpyAsync(n->x32, x, pix * n->L * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    k_f32_to_bf16<<<nblocks(pix * n->L), kThreads, 0, s>>>(x, n->a[0], pix * n->L);
+    GINF_WCK(cudaGetLastError());
+    for (int l = 0; l < 3; ++l)
+        GINF_WCK(conv_fwd(n->cin[l], n->cout[l], true, false, n->a[l], n->wbf + n->woff[l], n->params + n->boff[l], g,
+                          n->a[l + 1], nullptr, s));
+    GINF_WCK(conv_fwd(n->cin[3], n->cout[3], false, true, n->a[3], n->wbf + n->woff[3], n->params + n->boff[3], g,
+                      n->y, n->x32, s));
+    return GINF_OK;
+}
+
+// Loss and every parameter gradient (into n->grads) for one batch.
+ginf_status backward(ginf_warmnet *n, const float *target, Geo g, cudaStream_t s) {
+    const size_t pix = (size_t)g.n * g.h * g.w;
+    const size_t ny = pix * n->L;
+    int blocks = (int)std::min<size_t>(1024, nblocks(ny));
+    k_mse<<<blocks, kThreads, 0, s>>>(n->y, target, ny, n->gy, n->loss_part);
+    k_sum_double<<<1, 32, 0, s>>>(n->loss_part, blocks, (double)ny, n->loss_dev);
+    GINF_WCK(cudaGetLastError());
+    const int chunks = (int)((pix + kChunk - 1) / kChunk);
+    // Layer 4 (linear output): g = dy.
+    const float *gl = n->gy;
+    k_f32_to_bf16<<<nblocks(ny), kThreads, 0, s>>>(n->gy, n->gb, ny);
+    GINF_WCK(cudaGetLastError());
+    for (int l = 3; l >= 0; --l) {
+        const int ci = n->cin[l], co = n->cout[l];
+        // bias gradient
+        k_bias_partials<<<chunks, 128, 0, s>>>(gl, (int)pix, co, n->partials);
+        k_reduce_partials<<<nblocks(co), kThreads, 0, s>>>(n->partials, chunks, co, n->grads + n->boff[l]);
+        GINF_WCK(cudaGetLastError());
+        // weight gradient
+        GINF_WCK(conv_wgrad(ci, co, n->gb, n->a[l], g, n->partials, n->grads + n->woff[l], s));
+        if (l == 0) break;
+        // data gradient: conv of the (BF16) output gradient with the flipped weights
+        k_flip_weights<<<nblocks((size_t)ci * 9 * co), kThreads, 0, s>>>(n->wbf + n->woff[l], ci, co, n->wflip);
+        GINF_WCK(cudaGetLastError());
+        GINF_WCK(conv_fwd(co, ci, false, true, n->gb, n->wflip, nullptr, g, n->gtmp, nullptr, s));
+        // through the ReLU of layer l-1's output
+        k_relu_bwd<<<nblocks(pix * ci), kThreads, 0, s>>>(n->gtmp, n->a[l], pix * ci, n->g32, n->gb);
+        GINF_WCK(cudaGetLastError());
+        gl = n->g32;
+    }
+    return GINF_OK;
+}
+
+ginf_status check_geo(const ginf_warmnet *n, int nimg, int h, int w) {
+    if (!n) return wfail(GINF_ERR_INVALID_ARGUMENT, "warmnet is NULL");
+    if (nimg < 1 || h < 1 || w < 1) return wfail(GINF_ERR_INVALID_ARGUMENT, "bad batch geometry");
+    return GINF_OK;
+}
+
+const char kMagic[8] = {'G', 'I', 'N', 'F', 'W', 'N', 'E', 'T'};
+constexpr uint32_t kVersion = 1;
+
+}  // namespace
+
+namespace ginf_gpu {
+// Used by the learned HBP solve in capi.cu: forward pass on level-t inputs.
+ginf_status warmnet_forward(ginf_warmnet *n, const float *x, int nimg, int h, int w, float **y_out, cudaStream_t s) {
+    ginf_status st = check_geo(n, nimg, h, w);
+    if (st != GINF_OK) return st;
+    Geo g{nimg, h, w};
+    st = forward(n, x, g, s);
+    if (st != GINF_OK) return st;
+    *y_out = n->y;
+    return GINF_OK;
+}
+int warmnet_labels(const ginf_warmnet *n) { return n ? n->L : 0; }
+}  // namespace ginf_gpu
+
+extern "C" {
+
+ginf_status ginf_warmnet_create(ginf_warmnet **out, int32_t num_labels, int32_t hidden, uint64_t seed) {
+    ginf_gpu::set_last_error("");
+    if (!out) return wfail(GINF_ERR_INVALID_ARGUMENT, "out is NULL");
+    if ((num_labels != 16 && num_labels != 32 && num_labels != 64) || hidden != 32)
+        return wfail(GINF_ERR_UNSUPPORTED, "the warm-start network is compiled for L in {16, 32, 64} and 32 hidden channels");
+    ginf_warmnet *n = new ginf_warmnet();
+    n->L = num_labels;
+    n->hidden = hidden;
+    layout(n);
+    ginf_status st = alloc_params(n);
+    if (st != GINF_OK) {
+        ginf_warmnet_destroy(n);
+        return st;
+    }
+    // He-uniform weights (last layer scaled by 0.1), zero biases.
+    std::vector<float> p(n->nparams, 0.f);
+    uint64_t s = seed * 0x9E3779B97F4A7C15ull + 12345;
+    for (int l = 0; l < 4; ++l) {
+        const float bound = std::sqrt(6.f / (9.f * n->cin[l])) * (l == 3 ? 0.1f : 1.f);
+        for (size_t i = 0; i < (size_t)n->cout[l] * 9 * n->cin[l]; ++i) {
+            const double u = (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0);
+            p[n->woff[l] + i] = (float)((2.0 * u - 1.0) * bound);
+        }
+    }
+    if (cudaMemcpy(n->params, p.data(), p.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        refresh_bf16(n, nullptr) != GINF_OK || cudaDeviceSynchronize() != cudaSuccess) {
+        cudaGetLastError();
+        ginf_warmnet_destroy(n);
+        return wfail(GINF_ERR_CUDA, "warmnet initialisation failed");
+    }
+    *out = n;
+    return GINF_OK;
+}
+
+ginf_status ginf_warmnet_destroy(ginf_warmnet *n) {
+    if (!n) return GINF_OK;
+    cudaFree(n->params);
+    cudaFree(n->adam_m);
+    cudaFree(n->adam_v);
+    cudaFree(n->grads);
+    cudaFree(n->wbf);
+    cudaFree(n->wflip);
+    for (int l = 0; l < 4; ++l) cudaFree(n->a[l]);
+    cudaFree(n->x32);
+    cudaFree(n->y);
+    cudaFree(n->gy);
+    cudaFree(n->g32);
+    cudaFree(n->gtmp);
+    cudaFree(n->gb);
+    cudaFree(n->partials);
+    cudaFree(n->loss_part);
+    cudaFree(n->loss_dev);
+    delete n;
+    return GINF_OK;
+}
+
+ginf_status ginf_warmnet_num_params(const ginf_warmnet *n, int64_t *count) {
+    if (!n || !count) return wfail(GINF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *count = (int64_t)n->nparams;
+    return GINF_OK;
+}
+
+ginf_status ginf_warmnet_get_params(const ginf_warmnet *n, float *host) {
+    if (!n || !host) return wfail(GINF_ERR_INVALID_ARGUMENT, "NULL argument");
+    GINF_WCK(cudaMemcpy(host, n->params, n->nparams * sizeof(float), cudaMemcpyDeviceToHost));
+    return GINF_OK;
+}
+
+ginf_status ginf_warmnet_set_params(ginf_warmnet *n, const float *host) {
+    if (!n || !host) return wfail(GINF_ERR_INVALID_ARGUMENT, "NULL argument");
+    GINF_WCK(cudaMemcpy(n->params, host, n->nparams * sizeof(float), cudaMemcpyHostToDevice));
+    ginf_status st = refresh_bf16(n, nullptr);
+    if (st != GINF_OK) return st;
+    GINF_WCK(cudaDeviceSynchronize());
+    return GINF_OK;
+}
+
+ginf_status ginf_warmnet_forward(ginf_warmnet *n, const float *x, int32_t nimg, int32_t h, int32_t w, float *out,
+                                 void *stream) {
+    ginf_gpu::set_last_error("");
+    float *y = nullptr;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    ginf_status st = warmnet_forward(n, x, nimg, h, w, &y, s);
+    if (st != GINF_OK) return st;
+    GINF_WCK(cudaMemcpyAsync(out, y, (size_t)nimg * h * w * n->L * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    GINF_WCK(cudaStreamSynchronize(s));
+    return GINF_OK;
+}
+
+ginf_status ginf_warmnet_gradients(ginf_warmnet *n, const float *x, const float *target, int32_t nimg, int32_t h,
+                                   int32_t w, float *loss, float *grads_host, void *stream) {
+    ginf_gpu::set_last_error("");
+    ginf_status st = check_geo(n, nimg, h, w);
+    if (st != GINF_OK) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Geo g{nimg, h, w};
+    if ((st = forward(n, x, g, s)) != GINF_OK) return st;
+    if ((st = backward(n, target, g, s)) != GINF_OK) return st;
+    if (loss) GINF_WCK(cudaMemcpyAsync(loss, n->loss_dev, sizeof(float), cudaMemcpyDeviceToHost, s));
+    if (grads_host)
+        GINF_WCK(cudaMemcpyAsync(grads_host, n->grads, n->nparams * sizeof(float), cudaMemcpyDeviceToHost, s));
+    GINF_WCK(cudaStreamSynchronize(s));
+    return GINF_OK;
+}
+
+ginf_status ginf_warmnet_train_step(ginf_warmnet *n, const float *x, const float *target, int32_t nimg, int32_t h,
+                                    int32_t w, float lr, float *loss, void *stream) {
+    ginf_gpu::set_last_error("");
+    ginf_status st = check_geo(n, nimg, h, w);
+    if (st != GINF_OK) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Geo g{nimg, h, w};
+    if ((st = forward(n, x, g, s)) != GINF_OK) return st;
+    if ((st = backward(n, target, g, s)) != GINF_OK) return st;
+    n->step += 1;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - std::pow(b1, (float)n->step), c2 = 1.f - std::pow(b2, (float)n->step);
+    k_adam<<<nblocks(n->nparams), kThreads, 0, s>>>(n->params, n->grads, n->adam_m, n->adam_v, (int)n->nparams, lr,
+                                                    b1, b2, 1e-8f, c1, c2, n->wbf);
+    GINF_WCK(cudaGetLastError());
+    if (loss) GINF_WCK(cudaMemcpyAsync(loss, n->loss_dev, sizeof(float), cudaMemcpyDeviceToHost, s));
+    GINF_WCK(cudaStreamSynchronize(s));
+    return GINF_OK;
+}
+
+// Checkpoint: magic "GINFWNET", u32 version, u32 L, u32 hidden, i64 Adam step,
+// u64 parameter count, then parameters, Adam m and Adam v as FP32, then the
+// FNV-1a 64 checksum of everything before it.
+ginf_status ginf_warmnet_save(const ginf_warmnet *n, const char *path) {
+    if (!n || !path) return wfail(GINF_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::vector<unsigned char> buf;
+    auto put = [&](const void *p, size_t k) {
+        const unsigned char *c = static_cast<const unsigned char *>(p);
+        buf.insert(buf.end(), c, c + k);
+    };
+    const uint32_t ver = kVersion, L = (uint32_t)n->L, hid = (uint32_t)n->hidden;
+    const uint64_t np = n->nparams;
+    put(kMagic, 8);
+    put(&ver, 4);
+    put(&L, 4);
+    put(&hid, 4);
+    put(&n->step, 8);
+    put(&np, 8);
+    std::vector<float> tmp(np);
+    for (float *src : {n->params, n->adam_m, n->adam_v}) {
+        GINF_WCK(cudaMemcpy(tmp.data(), src, np * sizeof(float), cudaMemcpyDeviceToHost));
+        put(tmp.data(), np * sizeof(float));
+    }
+    const uint64_t sum = fnv1a(buf.data(), buf.size());
+    put(&sum, 8);
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return wfail(GINF_ERR_INVALID_ARGUMENT, std::string("cannot write ") + path);
+    const bool ok = std::fwrite(buf.data(), 1, buf.size(), f) == buf.size();
+    std::fclose(f);
+    if (!ok) return wfail(GINF_ERR_INVALID_ARGUMENT, std::string("short write to ") + path);
+    return GINF_OK;
+}
+
+ginf_status ginf_warmnet_load(ginf_warmnet **out, const char *path) {
+    ginf_gpu::set_last_error("");
+    if (!out || !path) return wfail(GINF_ERR_INVALID_ARGUMENT, "NULL argument");
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return wfail(GINF_ERR_INVALID_ARGUMENT, std::string("cannot read ") + path);
+    std::vector<unsigned char> buf;
+    unsigned char tmp[65536];
+    size_t k;
+    while ((k = std::fread(tmp, 1, sizeof(tmp), f)) > 0) buf.insert(buf.end(), tmp, tmp + k);
+    std::fclose(f);
+    const size_t head = 8 + 4 + 4 + 4 + 8 + 8;
+    if (buf.size() < head + 8 || std::memcmp(buf.data(), kMagic, 8) != 0)
+        return wfail(GINF_ERR_INVALID_ARGUMENT, "not a warm-start network file");
+    uint64_t sum;
+    std::memcpy(&sum, buf.data() + buf.size() - 8, 8);
+    if (sum != fnv1a(buf.data(), buf.size() - 8))
+        return wfail(GINF_ERR_INVALID_ARGUMENT, "warm-start network file: checksum mismatch");
+    uint32_t ver, L, hid;
+    int64_t step;
+    uint64_t np;
+    std::memcpy(&ver, buf.data() + 8, 4);
+    std::memcpy(&L, buf.data() + 12, 4);
+    std::memcpy(&hid, buf.data() + 16, 4);
+    std::memcpy(&step, buf.data() + 20, 8);
+    std::memcpy(&np, buf.data() + 28, 8);
+    if (ver != kVersion) return wfail(GINF_ERR_UNSUPPORTED, "warm-start network file: unknown version");
+    ginf_warmnet *n = nullptr;
+    ginf_status st = ginf_warmnet_create(&n, (int32_t)L, (int32_t)hid, 0);
+    if (st != GINF_OK) return st;
+    if (np != n->nparams || buf.size() != head + 3 * np * sizeof(float) + 8) {
+        ginf_warmnet_destroy(n);
+        return wfail(GINF_ERR_INVALID_ARGUMENT, "warm-start network file: size mismatch");
+    }
+    const unsigned char *p = buf.data() + head;
+    float *dst[3] = {n->params, n->adam_m, n->adam_v};
+    for (int i = 0; i < 3; ++i) {
+        if (cudaMemcpy(dst[i], p + (size_t)i * np * sizeof(float), np * sizeof(float), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            ginf_warmnet_destroy(n);
+            return wfail(GINF_ERR_CUDA, "warm-start network upload failed");
+        }
+    }
+    n->step = step;
+    if ((st = refresh_bf16(n, nullptr)) != GINF_OK || cudaDeviceSynchronize() != cudaSuccess) {
+        ginf_warmnet_destroy(n);
+        return st != GINF_OK ? st : wfail(GINF_ERR_CUDA, "warm-start network upload failed");
+    }
+    *out = n;
+    return GINF_OK;
+}
+
+}  // extern "C"

@@ -106,6 +106,7 @@ typedef struct ginf_stats {
     int64_t level0_sweep_launches;
     int64_t node_label_iters; /* sum over levels of W_t*H_t*L*iterations       */
     int64_t h2d_bytes, d2h_bytes;
+    int64_t warm_start_used;  /* learned solve: 1 = warm start kept, 0 = fell back */
 } ginf_stats;
 
 typedef struct ginf_workspace ginf_workspace;
@@ -191,6 +192,67 @@ ginf_status ginf_batch_config(const ginf_batch *batch, int32_t *tile_nodes, int3
 ginf_status ginf_batch_destroy(ginf_batch *batch);
 /* Create, run once, destroy. */
 ginf_status ginf_decode_bp_batch(const ginf_grid *grids, int32_t *const *labels, int32_t count, int32_t iters,
+                                 const ginf_options *opt, ginf_stats *stats);
+
+/* Learned warm start for hierarchical BP (new here: the reference has no
+ * learned component).  A small BF16 convolutional network (3x3 convs,
+ * L -> 32 -> 32 -> 32 -> L, ReLU, FP32 accumulate, tensor-core kernels) maps
+ * the costs of pyramid level t, x = D_t / 4^t, to that level's beliefs,
+ * y = x + net(x) ~ B_t / 4^t.  Device buffers are FP32, [n][h][w][L]. */
+typedef struct ginf_warmnet ginf_warmnet;
+ginf_status ginf_warmnet_create(ginf_warmnet **net, int32_t num_labels, int32_t hidden, uint64_t seed);
+/* Checkpoints hold the weights and the Adam state, with a checksum. */
+ginf_status ginf_warmnet_load(ginf_warmnet **net, const char *path);
+ginf_status ginf_warmnet_save(const ginf_warmnet *net, const char *path);
+ginf_status ginf_warmnet_destroy(ginf_warmnet *net);
+ginf_status ginf_warmnet_num_params(const ginf_warmnet *net, int64_t *count);
+/* FP32 parameters, per layer the weights [cout][3][3][cin] then the biases. */
+ginf_status ginf_warmnet_get_params(const ginf_warmnet *net, float *host);
+ginf_status ginf_warmnet_set_params(ginf_warmnet *net, const float *host);
+ginf_status ginf_warmnet_forward(ginf_warmnet *net, const float *x, int32_t n, int32_t h, int32_t w, float *y,
+                                 void *stream);
+/* Mean-squared-error loss against target and the gradient of every
+ * parameter (same order as get_params), without an update. */
+ginf_status ginf_warmnet_gradients(ginf_warmnet *net, const float *x, const float *target, int32_t n, int32_t h,
+                                   int32_t w, float *loss, float *grads_host, void *stream);
+/* One Adam step (beta 0.9 / 0.999) on the mean-squared-error loss. */
+ginf_status ginf_warmnet_train_step(ginf_warmnet *net, const float *x, const float *target, int32_t n, int32_t h,
+                                    int32_t w, float lr, float *loss, void *stream);
+/* Training data from this library's own BP: the network input of pyramid
+ * level `level` (x = D_t / 4^t) and, when beliefs_out is given, a target:
+ * target 0 = the level's beliefs / 4^t after hierarchical BP from the top of
+ * a num_levels pyramid down to that level; target 1 = (D_t + m) / 4^t after
+ * the whole schedule down to level 0, m being the mean over the node's
+ * 2^t x 2^t fine block of the level-0 incoming-message sums.  Device buffers
+ * [H_t][W_t][L]. */
+ginf_status ginf_hbp_level_state(ginf_workspace *ws, const ginf_grid *grid, int32_t num_levels,
+                                 int32_t iters_per_level, int32_t level, int32_t target, float *x_out,
+                                 float *beliefs_out, const ginf_options *opt);
+/* Hierarchical BP warm-started at level warm_level (1 <= warm_level <=
+ * num_levels - 2): the network reads that level's costs (x = D_t / 4^t) and
+ * its prediction y sets the level's messages (each incoming slot = 4^t/4 *
+ * (y - x)); warm_iters half-sweeps run there (0: the messages go down
+ * unchanged), levels warm_level-1 .. 1 run mid_iters (< 0: iters_per_level)
+ * and level 0 iters_per_level, as in ginf_decode_hbp.
+ * Fallback: the cold schedule first runs its levels down to warm_level+1
+ * (the cheap ones); when the seeded result has a higher level-0 energy than
+ * that level's labelling handed down to level 0, the seeded result is
+ * discarded and the cold schedule resumes, giving exactly ginf_decode_hbp's
+ * labels (stats->warm_start_used tells which). */
+ginf_status ginf_decode_hbp_learned(ginf_workspace *ws, const ginf_grid *grid, int32_t num_levels,
+                                    int32_t iters_per_level, int32_t warm_level, int32_t warm_iters,
+                                    int32_t mid_iters, ginf_warmnet *net, int32_t *labels,
+                                    const ginf_options *opt, ginf_stats *stats);
+
+/* As ginf_decode_hbp_learned with the prediction supplied by the caller: a
+ * device buffer [H_t][W_t][L] on the network's output scale (x = D_t / 4^t
+ * plus the predicted message sum / 4^t).  Levels warm_level-1 .. 1 run
+ * mid_iters half-sweeps (< 0: iters_per_level), level 0 iters_per_level.
+ * fallback = 0 always keeps the seeded result (no cold pass; warm_level may
+ * then be num_levels - 1). */
+ginf_status ginf_decode_hbp_warm(ginf_workspace *ws, const ginf_grid *grid, int32_t num_levels,
+                                 int32_t iters_per_level, int32_t warm_level, int32_t warm_iters,
+                                 int32_t mid_iters, const float *prediction, int32_t fallback, int32_t *labels,
                                  const ginf_options *opt, ginf_stats *stats);
 
 /* Loopy BP (one level, the reference message rule and stale-belief decode)

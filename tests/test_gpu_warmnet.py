@@ -1,0 +1,217 @@
+"""The warm-start network's tensor-core kernels against the CPU oracle
+(forward and every parameter gradient), its training step and checkpoints,
+and the learned hierarchical BP solve with its fallback."""
+import numpy as np
+import pytest
+
+from gridinfcuda_gb300 import synth
+from oracle import warmnet_ref as REF
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+
+
+@pytest.mark.parametrize("L", [16, 32, 64])
+def test_forward_matches_oracle(ginf, L):
+    import torch
+    params = REF.init_params(L, seed=L)
+    rng = np.random.default_rng(L)
+    x = rng.uniform(0, 1, (2, 9, 7, L)).astype(np.float32)
+    with ginf.WarmNet(L, 32) as net:
+        net.set_params(params)
+        y = net.forward(torch.from_numpy(x).cuda()).cpu().numpy()
+    want, _ = REF.forward(params, x, L)
+    assert _rel(y, want) < 1e-4
+
+
+@pytest.mark.parametrize("L", [16, 64])
+def test_gradients_match_oracle(ginf, L):
+    """Gradient check: loss within 1e-5 and every layer's weight and bias
+    gradients within 5e-3 (norm-relative) of the float64 oracle that rounds
+    to BF16 at the same points."""
+    import torch
+    params = REF.init_params(L, seed=7)
+    rng = np.random.default_rng(11)
+    x = rng.uniform(0, 1, (3, 10, 13, L)).astype(np.float32)
+    t = (x + rng.normal(0, 0.2, x.shape)).astype(np.float32)
+    with ginf.WarmNet(L, 32) as net:
+        net.set_params(params)
+        loss, g = net.gradients(torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda())
+    want_loss, want_g = REF.gradients(params, x, t, L)
+    assert abs(loss - want_loss) <= 1e-5 * abs(want_loss)
+    off = 0
+    for cin, cout in REF.shapes(L):
+        nw = cout * 9 * cin
+        assert _rel(g[off:off + nw], want_g[off:off + nw]) < 5e-3, ("weights", cin, cout)
+        assert _rel(g[off + nw:off + nw + cout], want_g[off + nw:off + nw + cout]) < 5e-3, ("bias", cin, cout)
+        off += nw + cout
+
+
+def test_training_lowers_the_loss(ginf):
+    import torch
+    rng = np.random.default_rng(5)
+    x = torch.from_numpy(rng.uniform(0, 1, (8, 12, 16, 16)).astype(np.float32)).cuda()
+    t = x + 0.3 * torch.roll(x, 1, dims=3)
+    with ginf.WarmNet(16, 32, seed=3) as net:
+        first = net.train_step(x, t, 3e-3)
+        for _ in range(60):
+            last = net.train_step(x, t, 3e-3)
+    assert last < 0.5 * first
+
+
+def test_checkpoint_resume_is_exact(ginf, tmp_path):
+    import torch
+    rng = np.random.default_rng(9)
+    x = torch.from_numpy(rng.uniform(0, 1, (4, 8, 8, 32)).astype(np.float32)).cuda()
+    t = x * 1.5 - 0.2
+    with ginf.WarmNet(32, 32, seed=1) as a:
+        for _ in range(10):
+            a.train_step(x, t, 1e-3)
+        straight = a.get_params()
+    with ginf.WarmNet(32, 32, seed=1) as b:
+        for _ in range(5):
+            b.train_step(x, t, 1e-3)
+        b.save(tmp_path / "ck.bin")
+    with ginf.WarmNet(path=tmp_path / "ck.bin") as c:
+        for _ in range(5):
+            c.train_step(x, t, 1e-3)
+        resumed = c.get_params()
+    assert np.array_equal(straight.view(np.uint32), resumed.view(np.uint32))
+    raw = bytearray(open(tmp_path / "ck.bin", "rb").read())
+    raw[100] ^= 0xFF
+    open(tmp_path / "bad.bin", "wb").write(bytes(raw))
+    with pytest.raises(ginf.GinfError) as e:
+        ginf.WarmNet(path=tmp_path / "bad.bin")
+    assert b"checksum" in str(e.value).encode()
+
+
+def test_level_state_inputs_and_beliefs(ginf, orc):
+    import torch
+    P = synth.random_problem(45, 37, 16, 2)
+    D, V = torch.from_numpy(P.D).cuda(), torch.from_numpy(P.V).cuda()
+    x, b = ginf.level_state(D, V, P.model, 3, 0, 2)
+    d = orc.pyramid(orc.pyramid(P.D))                   # (L, H2, W2)
+    want = np.transpose(d, (1, 2, 0)) / 16.0
+    assert np.array_equal(x.cpu().numpy(), want.astype(np.float32))
+    assert torch.equal(x, b)                            # no sweeps: beliefs are the costs
+    _, b2 = ginf.level_state(D, V, P.model, 3, 6, 2)
+    assert not torch.equal(x, b2)
+
+
+def _stereo(W=160, H=120, L=16, seed=4):
+    import torch
+    P = synth.stereo_problem(W, H, L, seed=seed, n_regions=6, sigma=2.0, planar=True, coef=0.07, cap=15.0,
+                             model=synth.TRUNC_LINEAR, scale=1.0, trunc=2.0)
+    return P, torch.from_numpy(P.D).cuda(), torch.from_numpy(P.V).cuda()
+
+
+def test_learned_solve_with_zero_network(ginf):
+    """A network that predicts zero messages: the warm level starts from zero
+    messages, i.e. a shorter pyramid.  The labels equal one of the two plain
+    schedules exactly, the one the fallback rule picks."""
+    P, D, V = _stereo()
+    with ginf.WarmNet(16, 32) as net:
+        net.set_params(np.zeros(net.num_params(), np.float32))
+        lab, st = ginf.decode_hbp_learned(D, V, P.model, 4, 6, 2, net, want_stats=True)
+    lab = lab.cpu().numpy()
+    short = ginf.decode_hbp(P.D, P.V, P.model, 3, 6)
+    full = ginf.decode_hbp(P.D, P.V, P.model, 4, 6)
+    want = short if st["warm_start_used"] else full
+    assert np.array_equal(lab[1:-1, 1:-1], want[1:-1, 1:-1])
+
+
+def test_learned_solve_falls_back_from_a_bad_network(ginf):
+    """Wild predictions and one half-sweep per level: the seeded result is
+    worse than the cold coarse labelling, so the cold schedule resumes and
+    the result equals plain HBP exactly."""
+    P, D, V = _stereo(seed=8)
+    with ginf.WarmNet(16, 32, seed=5) as net:
+        p = net.get_params()
+        p *= 1000.0
+        net.set_params(p)
+        lab, st = ginf.decode_hbp_learned(D, V, P.model, 4, 1, 2, net, want_stats=True)
+    assert st["warm_start_used"] == 0
+    full = ginf.decode_hbp(P.D, P.V, P.model, 4, 1)
+    assert np.array_equal(lab.cpu().numpy()[1:-1, 1:-1], full[1:-1, 1:-1])
+
+
+def _block_target(orc, D, M, t):
+    """(D_t + block mean of the level-0 incoming-message sums) / 4^t in
+    float32, accumulated in the kernel's order: block rows, block columns,
+    then directions S, E, N, W."""
+    L, H, W = D.shape
+    Dt = D
+    for _ in range(t):
+        Dt = orc.pyramid(Dt)
+    _, Ht, Wt = Dt.shape
+    bs = 1 << t
+    out = np.zeros((Ht, Wt, L), np.float32)
+    for Y in range(Ht):
+        for X in range(Wt):
+            acc = np.zeros(L, np.float32)
+            cnt = 0
+            for y in range(Y * bs, min(H, (Y + 1) * bs)):
+                for x in range(X * bs, min(W, (X + 1) * bs)):
+                    for d in range(4):
+                        acc = (acc + M[y, x, d]).astype(np.float32)
+                    cnt += 1
+            mean = (acc / np.float32(cnt)).astype(np.float32)
+            out[Y, X] = ((Dt[:, Y, X] + mean).astype(np.float32) / np.float32(bs * bs)).astype(np.float32)
+    return out
+
+
+def test_level_state_fine_target(ginf, orc):
+    """target 1: the level-0 messages of the whole schedule, averaged per
+    level-t block, plus the level-t costs, over 4^t -- bit for bit."""
+    import torch
+    P = synth.random_problem(37, 29, 16, 2)
+    D, V = torch.from_numpy(P.D).cuda(), torch.from_numpy(P.V).cuda()
+    for t in (1, 2):
+        x, y = ginf.level_state(D, V, P.model, 3, 5, t, target=1)
+        _, M = ginf.decode_hbp(P.D, P.V, P.model, 3, 5, want_msgs=True)
+        want = _block_target(orc, P.D, M, t)
+        assert np.array_equal(y.cpu().numpy(), want), t
+
+
+def test_seed_of_zero_messages_is_a_shorter_pyramid(ginf):
+    """decode_hbp_warm with y = x (zero messages) at level t, no fallback,
+    warm_iters = iters: exactly plain HBP with t + 1 levels."""
+    import torch
+    P, D, V = _stereo(seed=3)
+    for t in (1, 2):
+        x, _ = ginf.level_state(D, V, P.model, 4, 0, t, want_beliefs=False)
+        lab = ginf.decode_hbp_warm(D, V, P.model, 4, 5, t, x, warm_iters=5, fallback=False)
+        want = ginf.decode_hbp(P.D, P.V, P.model, t + 1, 5)
+        assert np.array_equal(lab.cpu().numpy()[1:-1, 1:-1], want[1:-1, 1:-1]), t
+    with pytest.raises(ValueError):
+        ginf.decode_hbp_warm(D, V, P.model, 4, 5, 1, torch.zeros((3, 3, 16), device="cuda"))
+
+
+def test_converged_seed_is_kept_and_converges_fast(ginf):
+    """Seeding level 1 with the converged fine-level messages: the fallback
+    keeps it and two half-sweeps at level 0 land within 0.5 % of the
+    converged energy, where the cold start with two is far off."""
+    P, D, V = _stereo(W=320, H=240, L=16, seed=6)
+    lab = ginf.decode_hbp(D, V, P.model, 5, 50)
+    e_star = ginf.energy(D, V, P.model, lab)
+    _, y = ginf.level_state(D, V, P.model, 5, 40, 1, target=1)
+    lab, st = ginf.decode_hbp_warm(D, V, P.model, 5, 2, 1, y, warm_iters=0, mid_iters=0, want_stats=True)
+    assert st["warm_start_used"] == 1
+    e_warm = ginf.energy(D, V, P.model, lab)
+    e_cold = ginf.energy(D, V, P.model, ginf.decode_hbp(D, V, P.model, 5, 2))
+    assert e_warm <= 1.005 * e_star < e_cold
+
+
+def test_bad_seed_falls_back_to_plain_hbp(ginf):
+    """A seed of zero messages at level 1 with two half-sweeps at level 0 is
+    worse than the cold level-2 labelling: the result is plain HBP."""
+    P, D, V = _stereo(W=320, H=240, L=16, seed=6)
+    x, _ = ginf.level_state(D, V, P.model, 5, 0, 1, want_beliefs=False)
+    lab, st = ginf.decode_hbp_warm(D, V, P.model, 5, 2, 1, x, warm_iters=0, mid_iters=0, want_stats=True)
+    want = ginf.decode_hbp(P.D, P.V, P.model, 5, 2)
+    assert st["warm_start_used"] == 0
+    assert np.array_equal(lab.cpu().numpy()[1:-1, 1:-1], want[1:-1, 1:-1])
