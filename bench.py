@@ -9,9 +9,13 @@ node-label-iterations per second, summed over the BP levels
 
   value     inputs resident in HBM; C-ABI ginf_solve on device buffers,
             timed with CUDA events on the stream the library runs on.
-  e2e       the same call with pinned HOST buffers: the host->device copy of
-            the costs and labels and the device->host copy of labels and
-            energy are inside the timed region.
+  e2e       the same solve with pinned HOST buffers, frames streamed
+            through the stream-ordered ginf_solve (two workspaces on two
+            streams): every frame's host->device copy of costs, table and
+            labels and device->host copy of labels and energy are inside the
+            timed region; one frame's copy overlaps the previous frame's
+            sweeps.  The one-synchronous-call-per-frame times are reported
+            beside it.
   roofline  the finest-level half-sweep kernel: algorithmic bytes (updated
             nodes x (L costs + 4L incoming + 4L outgoing) x 4 B) per launch
             over its mean launch duration, from CUDA events the library
@@ -25,6 +29,7 @@ oracle, all host threads) on the same workload and prints its own line.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -269,22 +274,62 @@ def run_ours(args, cfg):
     Vh = torch.from_numpy(P.V).pin_memory()
     labh = torch.zeros((cfg["H"], cfg["W"]), dtype=torch.int32).pin_memory()
 
-    def step_host():
+    def step_host(access):
         return capi.solve(Dh, Vh, P.model, cfg["levels"], cfg["iters"], cfg["icm"], labels=labh, workspace=ws,
-                          want_stats=True, **opt)
+                          want_stats=True, host_access=access, **opt)
 
-    for _ in range(max(1, min(args.warmup, 2))):
-        step_host()
+    def time_e2e(access):
+        for _ in range(max(1, min(args.warmup, 2))):
+            step_host(access)
+        torch.cuda.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        est = None
+        for _ in range(args.steps):
+            _, _, est = step_host(access)
+        torch.cuda.synchronize()
+        return reduce_max(time.perf_counter() - t0, world, dev), est
+
+    # One synchronous call per frame: the device reads the pinned costs in
+    # place (the transfer fused into the layout transform), or they are
+    # staged by one host-to-device copy first.
+    sync_s, est = time_e2e(capi.HOST_AUTO)
+    copy_s, _ = time_e2e(capi.HOST_COPY)
+
+    # Frames streamed through the stream-ordered call: two workspaces on two
+    # streams, so frame i+1's host-to-device copy (copy engine) runs under
+    # frame i's sweeps.  Every frame still moves its costs in and its labels
+    # and energy out inside the timed region.
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    wss = [ws, capi.Workspace()]
+    labs = [labh, torch.zeros_like(labh).pin_memory()]
+    energies = [ctypes.c_double(), ctypes.c_double()]
+
+    frame_opt = {k: v for k, v in opt.items() if k != "stream"}
+
+    def frames(n):
+        for i in range(n):
+            k = i % 2
+            capi.solve_async(Dh, Vh, P.model, cfg["levels"], cfg["iters"], cfg["icm"], labs[k], energies[k], wss[k],
+                             streams[k].cuda_stream, host_access=capi.HOST_COPY, **frame_opt)
+        for w in wss:
+            w.sync()
+
+    frames(max(2, min(args.warmup, 4)))
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
-    est = None
-    for _ in range(args.steps):
-        _, _, est = step_host()
+    frames(args.steps)
     torch.cuda.synchronize()
-    e2e_s = reduce_max(time.perf_counter() - t0, world, dev)
-    e2e = {"value": world * args.steps * nli / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(est["h2d_bytes"]),
-           "d2h_bytes_per_step": int(est["d2h_bytes"]), "ms_per_step": round(e2e_s * 1e3 / args.steps, 3)}
+    pipe_s = reduce_max(time.perf_counter() - t0, world, dev)
+    if abs(energies[0].value - energies[1].value) > 1e-9 * abs(energies[0].value):
+        raise RuntimeError("stream-ordered frames disagree")
+    wss[1].close()
+    e2e = {"value": world * args.steps * nli / pipe_s, "unit": UNIT, "h2d_bytes_per_step": int(est["h2d_bytes"]),
+           "d2h_bytes_per_step": int(est["d2h_bytes"]), "ms_per_step": round(pipe_s * 1e3 / args.steps, 3),
+           "mode": "stream-ordered ginf_solve, 2 workspaces / 2 streams, pinned host buffers",
+           "sync_call_ms_per_step": round(sync_s * 1e3 / args.steps, 3),
+           "sync_call_staged_copy_ms_per_step": round(copy_s * 1e3 / args.steps, 3)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

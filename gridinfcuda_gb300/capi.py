@@ -21,6 +21,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libginf_gb3
 OK, ERR_INVALID_ARGUMENT, ERR_UNSUPPORTED, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_TIMEOUT, ERR_NO_DEVICE = range(7)
 F32, I32, F64 = 0, 1, 2
 HOST, DEVICE = 0, 1
+HOST_AUTO, HOST_COPY = 0, 1   # ginf_options.host_access
 RULE_REFERENCE, RULE_STANDARD = 0, 1
 STORE_NATIVE, STORE_F16 = 0, 1
 DECODE_STALE, DECODE_FRESH = 0, 1
@@ -39,7 +40,8 @@ class Grid(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("msg_rule", _i32), ("msg_store", _i32), ("decode", _i32), ("normalize", _i32),
                 ("compute_type", _i32), ("tile_nodes", _i32), ("sweeps_per_launch", _i32), ("autotune", _i32),
-                ("stream", _p), ("msgs_out", _p), ("reserved", ctypes.c_int64 * 6)]
+                ("stream", _p), ("msgs_out", _p), ("host_access", _i32), ("asynchronous", _i32),
+                ("reserved", ctypes.c_int64 * 5)]
 
 
 class Stats(ctypes.Structure):
@@ -73,6 +75,7 @@ def lib():
         L.ginf_default_options.argtypes = [ctypes.POINTER(Options)]
         L.ginf_workspace_create.argtypes = [ctypes.POINTER(_p)]
         L.ginf_workspace_destroy.argtypes = [_p]
+        L.ginf_workspace_sync.argtypes = [_p]
         L.ginf_decode_hbp.argtypes = [_p, ctypes.POINTER(Grid), _i32, _i32, _p, ctypes.POINTER(Options),
                                       ctypes.POINTER(Stats)]
         L.ginf_decode_icm.argtypes = [_p, ctypes.POINTER(Grid), _p, _i32, _i32, _p, ctypes.POINTER(Options),
@@ -112,7 +115,7 @@ def lib():
                      "ginf_warmnet_load", "ginf_warmnet_save", "ginf_warmnet_destroy", "ginf_warmnet_num_params",
                      "ginf_warmnet_get_params", "ginf_warmnet_set_params", "ginf_warmnet_forward",
                      "ginf_warmnet_gradients", "ginf_warmnet_train_step", "ginf_hbp_level_state",
-                     "ginf_decode_hbp_learned", "ginf_decode_hbp_warm"):
+                     "ginf_decode_hbp_learned", "ginf_decode_hbp_warm", "ginf_workspace_sync"):
             getattr(L, name).restype = _i32
         _lib = L
     return _lib
@@ -130,6 +133,11 @@ class Workspace:
         h = _p()
         check(lib().ginf_workspace_create(ctypes.byref(h)))
         self.handle = h
+
+    def sync(self):
+        """Waits for this workspace's stream-ordered calls; raises a device
+        error any of them recorded."""
+        check(lib().ginf_workspace_sync(self.handle))
 
     def close(self):
         if self.handle:
@@ -188,7 +196,8 @@ def make_grid(D, V, model):
 
 
 def options(rule=RULE_REFERENCE, store=STORE_NATIVE, decode=DECODE_STALE, normalize=NORM_MEAN, compute_type=-1,
-            tile_nodes=0, sweeps_per_launch=0, autotune=0, stream=None, msgs_out=None):
+            tile_nodes=0, sweeps_per_launch=0, autotune=0, stream=None, msgs_out=None, host_access=0,
+            asynchronous=0):
     o = Options()
     lib().ginf_default_options(ctypes.byref(o))
     o.msg_rule, o.msg_store, o.decode, o.normalize = rule, store, decode, normalize
@@ -196,6 +205,8 @@ def options(rule=RULE_REFERENCE, store=STORE_NATIVE, decode=DECODE_STALE, normal
     o.sweeps_per_launch, o.autotune = sweeps_per_launch, autotune
     o.stream = stream if stream is not None else None
     o.msgs_out = msgs_out
+    o.host_access = host_access
+    o.asynchronous = asynchronous
     return o
 
 
@@ -264,6 +275,17 @@ def solve(D, V, model, levels, iters, icm_iters, labels=None, *, workspace=None,
     check(lib().ginf_solve(ws, ctypes.byref(g), levels, iters, icm_iters, _ptr(lab)[0], ctypes.byref(e),
                            ctypes.byref(o), ctypes.byref(st) if want_stats else None))
     return (lab, e.value, st.as_dict()) if want_stats else (lab, e.value)
+
+
+def solve_async(D, V, model, levels, iters, icm_iters, labels, energy, workspace, stream, **opt):
+    """Stream-ordered ginf_solve: enqueues on `stream` (a cudaStream_t handle)
+    and returns.  `labels` receives the result and the ctypes.c_double
+    `energy` the FP64 energy once the stream (or workspace.sync()) is done;
+    D, V, labels and energy must stay alive and unchanged until then."""
+    g = make_grid(D, V, model)
+    o = options(stream=stream, asynchronous=1, **opt)
+    check(lib().ginf_solve(workspace.handle, ctypes.byref(g), levels, iters, icm_iters, _ptr(labels)[0],
+                           ctypes.byref(energy), ctypes.byref(o), None))
 
 
 def stereo_costs(left, right, L, coef, cap, out, stream=None):

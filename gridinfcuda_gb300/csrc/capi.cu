@@ -9,6 +9,7 @@
 #include <cuda_fp16.h>
 
 #include <cstdio>
+#include <atomic>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -82,6 +83,12 @@ struct ginf_workspace {
     double *energy_host = nullptr;  // pinned
     cudaEvent_t ev[10] = {};
     bool events = false;
+    // Stream-ordered calls: `done` is recorded behind the last one; later
+    // calls on this workspace order their stream after it.  Device status
+    // words of finished stream-ordered calls accumulate in `deferred`.
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+    std::atomic<int> deferred{0};
 };
 
 namespace {
@@ -103,7 +110,16 @@ ginf_status check_device(ginf_workspace *ws) {
     return GINF_OK;
 }
 
-ginf_status ws_init(ginf_workspace *ws) {
+ginf_status device_status_error(int st) {
+    if (st & DEV_ERR_TIMEOUT) return fail(GINF_ERR_TIMEOUT, "a device-side wait exceeded its time limit");
+    if (st & DEV_ERR_BOUNDS) return fail(GINF_ERR_INVALID_ARGUMENT, "a label is outside [0, num_labels)");
+    return GINF_OK;
+}
+
+// Readies the workspace for a call on `stream`: the stream waits for the
+// workspace's last stream-ordered call, and a device error that call
+// recorded is reported now.
+ginf_status ws_init(ginf_workspace *ws, cudaStream_t stream) {
     GINF_TRY(check_device(ws));
     if (!ws->status_host) {
         GINF_CK(cudaMallocHost(&ws->status_host, 64));
@@ -111,9 +127,11 @@ ginf_status ws_init(ginf_workspace *ws) {
     }
     if (!ws->events) {
         for (int i = 0; i < EV_COUNT; ++i) GINF_CK(cudaEventCreate(&ws->ev[i]));
+        GINF_CK(cudaEventCreateWithFlags(&ws->done, cudaEventDisableTiming));
         ws->events = true;
     }
-    return GINF_OK;
+    if (ws->pending) GINF_CK(cudaStreamWaitEvent(stream, ws->done, 0));
+    return device_status_error(ws->deferred.exchange(0));
 }
 
 // Carves sub-buffers out of one growing device allocation.
@@ -190,6 +208,8 @@ struct Resolved {
     int mode;       // Mode
     int norm_min;
     int decode;
+    int host_access;
+    int async;
     SweepConfig cfg;
     cudaStream_t stream;
 };
@@ -222,8 +242,35 @@ ginf_status resolve(const ginf_grid *g, const ginf_options *o, Resolved &r) {
     if (o->tile_nodes != 0 && o->tile_nodes != 8 && o->tile_nodes != 16 && o->tile_nodes != 32)
         return fail(GINF_ERR_INVALID_ARGUMENT, "tile_nodes must be 0, 8, 16 or 32");
     r.cfg.nt = o->tile_nodes == 0 ? 16 : o->tile_nodes;
+    if (o->host_access != GINF_HOST_AUTO && o->host_access != GINF_HOST_COPY)
+        return fail(GINF_ERR_INVALID_ARGUMENT, "unknown host_access");
+    r.host_access = o->host_access;
+    r.async = o->asynchronous != 0;
     r.stream = static_cast<cudaStream_t>(o->stream);
     return GINF_OK;
+}
+
+// A device-readable address of the host buffer p, or nullptr when the
+// device cannot read it in place: page-locked memory (its mapped device
+// pointer) or, where the device reads pageable memory coherently (Grace
+// systems), the pointer itself.
+const void *host_device_view(const void *p) {
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (pa.type == cudaMemoryTypeHost) return pa.devicePointer;
+    if (pa.type == cudaMemoryTypeUnregistered) {
+        int dev = 0, pageable = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return pageable ? p : nullptr;
+    }
+    return nullptr;
 }
 
 struct Level {
@@ -291,15 +338,18 @@ ginf_status prepare(Call &c, Prepared &P, int levels, bool want_lab2, const int3
     const size_t lab_bytes = (size_t)W * H * sizeof(int32_t);
     P.num_partials = energy_num_partials(W, H);
 
+    const bool host = g->memory == GINF_HOST;
+    // Host costs the device can read in place are read by the layout
+    // transform itself (the transfer fused into it); others are staged.
+    const void *host_view = host && c.r.host_access == GINF_HOST_AUTO ? host_device_view(g->data_costs) : nullptr;
     Arena a;
     const size_t id_rec = a.add(rec_total);
-    const size_t id_stage = g->memory == GINF_HOST ? a.add(cost_bytes) : 0;
+    const size_t id_stage = host && !host_view ? a.add(cost_bytes) : 0;
     const size_t id_tin = a.add(table_in);
     const size_t id_t = a.add(table_t);
     const size_t id_lab = (labels_dev == nullptr) ? a.add(lab_bytes) : 0;
     const size_t id_lab2 = want_lab2 ? a.add(lab_bytes) : 0;
     const size_t id_part = a.add(sizeof(double) * (P.num_partials + 1) + 64);
-    const bool host = g->memory == GINF_HOST;
     GINF_TRY(ws_reserve(c.ws, a.total()));
     unsigned char *base = c.ws->arena;
     P.rec = a.ptr(base, id_rec);
@@ -316,12 +366,16 @@ ginf_status prepare(Call &c, Prepared &P, int levels, bool want_lab2, const int3
     const void *costs_dev = g->data_costs;
     const void *table_dev = g->sm_costs;
     if (host) {
-        unsigned char *stage = a.ptr(base, id_stage);
-        GINF_CK(cudaMemcpyAsync(stage, g->data_costs, cost_bytes, cudaMemcpyHostToDevice, s));
+        if (host_view) {
+            costs_dev = host_view;
+        } else {
+            unsigned char *stage = a.ptr(base, id_stage);
+            GINF_CK(cudaMemcpyAsync(stage, g->data_costs, cost_bytes, cudaMemcpyHostToDevice, s));
+            costs_dev = stage;
+        }
         unsigned char *tin = a.ptr(base, id_tin);
         GINF_CK(cudaMemcpyAsync(tin, g->sm_costs, table_in, cudaMemcpyHostToDevice, s));
         c.h2d += cost_bytes + table_in;
-        costs_dev = stage;
         table_dev = tin;
     }
     if (labels_in) {
@@ -541,9 +595,50 @@ ginf_status finish(Call &c, int64_t nli) {
 ginf_status read_status(Call &c, Prepared &P) {
     GINF_CK(cudaMemcpyAsync(c.ws->status_host, P.status, sizeof(int), cudaMemcpyDeviceToHost, c.r.stream));
     GINF_CK(cudaStreamSynchronize(c.r.stream));
-    const int st = *c.ws->status_host;
-    if (st & DEV_ERR_TIMEOUT) return fail(GINF_ERR_TIMEOUT, "a device-side wait exceeded its time limit");
-    if (st & DEV_ERR_BOUNDS) return fail(GINF_ERR_INVALID_ARGUMENT, "a label is outside [0, num_labels)");
+    return device_status_error(*c.ws->status_host);
+}
+
+// Completion of a stream-ordered call, run by CUDA behind the call's work.
+struct Completion {
+    ginf_workspace *ws;
+    double *energy_out;
+};
+
+void CUDART_CB on_complete(void *p) {
+    Completion *d = static_cast<Completion *>(p);
+    const int st = *d->ws->status_host;
+    if (st) d->ws->deferred.fetch_or(st);
+    if (d->energy_out) *d->energy_out = *d->ws->energy_host;
+    delete d;
+}
+
+// Ends a call.  A synchronous call waits for its stream and reports the
+// device status; a stream-ordered call queues the status read (and the hand-
+// over of the energy to *energy_out) behind its work and returns at once.
+ginf_status complete(Call &c, Prepared &P, int64_t nli, double *energy_out) {
+    if (!c.r.async) {
+        GINF_TRY(read_status(c, P));
+        if (energy_out) *energy_out = *c.ws->energy_host;
+        return finish(c, nli);
+    }
+    cudaStream_t s = c.r.stream;
+    GINF_CK(cudaMemcpyAsync(c.ws->status_host, P.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    Completion *d = new Completion{c.ws, energy_out};
+    cudaError_t e = cudaLaunchHostFunc(s, on_complete, d);
+    if (e != cudaSuccess) {
+        delete d;
+        return cuda_fail(e, "cudaLaunchHostFunc");
+    }
+    GINF_CK(cudaEventRecord(c.ws->done, s));
+    c.ws->pending = true;
+    return GINF_OK;
+}
+
+// A stream-ordered call needs a caller-owned workspace and no stats.
+ginf_status check_async(const Call &c, const ginf_workspace *wsp) {
+    if (!c.r.async) return GINF_OK;
+    if (!wsp) return fail(GINF_ERR_INVALID_ARGUMENT, "a stream-ordered call needs a workspace");
+    if (c.stats) return fail(GINF_ERR_INVALID_ARGUMENT, "a stream-ordered call takes no stats");
     return GINF_OK;
 }
 
@@ -622,12 +717,25 @@ ginf_status ginf_workspace_create(ginf_workspace **ws) {
     return GINF_OK;
 }
 
+ginf_status ginf_workspace_sync(ginf_workspace *ws) {
+    g_last_error.clear();
+    if (!ws) return fail(GINF_ERR_INVALID_ARGUMENT, "ws is NULL");
+    if (ws->pending) {
+        GINF_CK(cudaEventSynchronize(ws->done));
+        ws->pending = false;
+    }
+    return device_status_error(ws->deferred.exchange(0));
+}
+
 ginf_status ginf_workspace_destroy(ginf_workspace *ws) {
     if (!ws) return GINF_OK;
+    if (ws->pending) cudaEventSynchronize(ws->done);
     if (ws->arena) cudaFree(ws->arena);
     if (ws->status_host) cudaFreeHost(ws->status_host);
-    if (ws->events)
+    if (ws->events) {
         for (int i = 0; i < EV_COUNT; ++i) cudaEventDestroy(ws->ev[i]);
+        cudaEventDestroy(ws->done);
+    }
     delete ws;
     return GINF_OK;
 }
@@ -647,7 +755,8 @@ ginf_status ginf_decode_hbp(ginf_workspace *wsp, const ginf_grid *grid, int32_t 
     c.ws = guard.ws;
     c.g = grid;
     c.stats = stats;
-    GINF_TRY(ws_init(c.ws));
+    GINF_TRY(check_async(c, wsp));
+    GINF_TRY(ws_init(c.ws, c.r.stream));
     begin(c);
     Prepared P;
     const bool host = grid->memory == GINF_HOST;
@@ -661,8 +770,7 @@ ginf_status ginf_decode_hbp(ginf_workspace *wsp, const ginf_grid *grid, int32_t 
     GINF_TRY(export_msgs(c, P, opt));
     GINF_TRY(labels_to_caller(c, P, labels, true));
     c.ev(EV_END);
-    GINF_TRY(read_status(c, P));
-    return finish(c, nli);
+    return complete(c, P, nli, nullptr);
 }
 
 ginf_status ginf_decode_icm(ginf_workspace *wsp, const ginf_grid *grid, const int32_t *initial, int32_t iters,
@@ -677,7 +785,7 @@ ginf_status ginf_decode_icm(ginf_workspace *wsp, const ginf_grid *grid, const in
     c.ws = guard.ws;
     c.g = grid;
     c.stats = stats;
-    GINF_TRY(ws_init(c.ws));
+    GINF_TRY(ws_init(c.ws, c.r.stream));
     begin(c);
     Prepared P;
     const bool host = grid->memory == GINF_HOST;
@@ -705,7 +813,7 @@ ginf_status ginf_energy(ginf_workspace *wsp, const ginf_grid *grid, const int32_
     c.ws = guard.ws;
     c.g = grid;
     c.stats = nullptr;
-    GINF_TRY(ws_init(c.ws));
+    GINF_TRY(ws_init(c.ws, c.r.stream));
     const int W = grid->width, H = grid->height, L = grid->num_labels;
     const bool host = grid->memory == GINF_HOST;
     const size_t ts = type_size(grid->cost_type);
@@ -760,7 +868,8 @@ ginf_status ginf_solve(ginf_workspace *wsp, const ginf_grid *grid, int32_t num_l
     c.ws = guard.ws;
     c.g = grid;
     c.stats = stats;
-    GINF_TRY(ws_init(c.ws));
+    GINF_TRY(check_async(c, wsp));
+    GINF_TRY(ws_init(c.ws, c.r.stream));
     begin(c);
     Prepared P;
     const bool host = grid->memory == GINF_HOST;
@@ -779,9 +888,7 @@ ginf_status ginf_solve(ginf_workspace *wsp, const ginf_grid *grid, int32_t num_l
         c.d2h += sizeof(double);
     }
     c.ev(EV_END);
-    GINF_TRY(read_status(c, P));
-    if (energy) *energy = *c.ws->energy_host;
-    return finish(c, nli);
+    return complete(c, P, nli, energy);
 }
 
 // The learned warm start needs FP32 arithmetic, the native store and the
@@ -808,7 +915,7 @@ ginf_status ginf_hbp_level_state(ginf_workspace *wsp, const ginf_grid *grid, int
     c.ws = guard.ws;
     c.g = grid;
     c.stats = nullptr;
-    GINF_TRY(ws_init(c.ws));
+    GINF_TRY(ws_init(c.ws, c.r.stream));
     Prepared P;
     GINF_TRY(prepare(c, P, num_levels, false, nullptr, nullptr));
     const Level &lt = P.lv[level];
@@ -868,7 +975,7 @@ static ginf_status decode_hbp_seeded(ginf_workspace *wsp, const ginf_grid *grid,
     c.ws = guard.ws;
     c.g = grid;
     c.stats = stats;
-    GINF_TRY(ws_init(c.ws));
+    GINF_TRY(ws_init(c.ws, c.r.stream));
     begin(c);
     Prepared P;
     GINF_TRY(prepare(c, P, num_levels, false, nullptr, labels));

@@ -58,6 +58,8 @@ enum { GINF_STORE_NATIVE = 0, GINF_STORE_F16 = 1 };
  * last update (bp.cc:65-84, 168-173); FRESH recomputes beliefs from the final
  * messages. */
 enum { GINF_DECODE_STALE = 0, GINF_DECODE_FRESH = 1 };
+/* How host-resident costs reach the device (ginf_options.host_access). */
+enum { GINF_HOST_AUTO = 0, GINF_HOST_COPY = 1 };
 /* Message normalisation: subtract the mean (bp.cc:50-54) or the minimum. */
 enum { GINF_NORM_MEAN = 0, GINF_NORM_MIN = 1 };
 
@@ -88,7 +90,22 @@ typedef struct ginf_options {
                                 compute type, slot d = message from the neighbour in
                                 direction d (0 where that neighbour is on the border
                                 or off the grid); same memory kind as the grid     */
-    int64_t reserved[6];
+    int32_t host_access;     /* GINF_HOST grids: GINF_HOST_AUTO (default) lets the
+                                device read the caller's costs in place when CUDA
+                                reports them device-accessible (pinned memory, or
+                                pageable memory on systems with pageable access),
+                                fusing the transfer into the layout transform;
+                                GINF_HOST_COPY always stages them by a copy      */
+    int32_t asynchronous;    /* ginf_decode_hbp / ginf_solve: 1 = stream-ordered.
+                                The call enqueues its work on `stream` and returns;
+                                host outputs (labels, energy) are valid once the
+                                stream or ginf_workspace_sync(ws) has finished, and
+                                the caller's host buffers must stay alive and
+                                unchanged until then.  Needs a caller-owned
+                                workspace and stats == NULL.  A device-side error
+                                is reported by ginf_workspace_sync or by the next
+                                call on the workspace.  Other calls ignore it.     */
+    int64_t reserved[5];
 } ginf_options;
 
 /* Per-call measurements (filled when a non-null pointer is passed; the call
@@ -122,6 +139,9 @@ void ginf_default_options(ginf_options *opt);
  * the reference does (src/gpu/bp.cu:141-222). */
 ginf_status ginf_workspace_create(ginf_workspace **ws);
 ginf_status ginf_workspace_destroy(ginf_workspace *ws);
+/* Waits for the workspace's stream-ordered calls and reports a device-side
+ * error any of them recorded. */
+ginf_status ginf_workspace_sync(ginf_workspace *ws);
 
 /* Hierarchical min-sum BP, num_levels == 1 being loopy BP.
  * Replaces ginf::decodeHbp (src/bp.cc:86-180), ginf::decodeBp (bp.cc:182-187),

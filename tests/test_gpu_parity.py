@@ -255,3 +255,56 @@ def test_wide_quadratic_lower_envelope_vs_fp64(ginf, orc):
     got, mg = ginf.decode_hbp(P.D, P.V, P.model, 1, 8, want_msgs=True, rule=ginf.RULE_STANDARD)
     assert _msg_rel_err(mg, mw) < 1e-4
     assert (got[1:-1, 1:-1] == want[1:-1, 1:-1]).mean() >= 0.999
+
+
+def test_host_costs_read_in_place_or_staged(ginf, orc):
+    """Host costs read in place by the device (page-locked memory, and
+    pageable memory where the device reads it coherently) or staged by a
+    copy: identical labels and messages, equal to the oracle's."""
+    import torch
+    P = synth.random_problem(97, 61, 24, 5)
+    want, msgs_want = orc.hbp(P.D, P.V, P.model, 3, 5, want_msgs=True)
+    pinned = (torch.from_numpy(P.D).pin_memory(), torch.from_numpy(P.V).pin_memory())
+    for D, V in ((P.D, P.V), pinned):
+        for access in (ginf.HOST_AUTO, ginf.HOST_COPY):
+            lab, msgs = ginf.decode_hbp(D, V, P.model, 3, 5, want_msgs=True, host_access=access)
+            lab, msgs = np.asarray(lab), np.asarray(msgs)
+            assert np.array_equal(lab[1:-1, 1:-1], want[1:-1, 1:-1]), (type(D), access)
+            assert np.array_equal(msgs.view(np.uint32), msgs_want.view(np.uint32)), (type(D), access)
+    with pytest.raises(ginf.GinfError):
+        ginf.decode_hbp(P.D, P.V, P.model, 3, 5, host_access=7)
+
+
+def test_stream_ordered_solve(ginf):
+    """Stream-ordered ginf_solve on two workspaces and two streams, pinned
+    host buffers: every frame equals the synchronous call; misuse is
+    rejected."""
+    import ctypes
+    import torch
+    P = synth.random_problem(150, 110, 32, 9)
+    want_lab, want_e = ginf.solve(P.D, P.V, P.model, 3, 6, 2)
+    D, V = torch.from_numpy(P.D).pin_memory(), torch.from_numpy(P.V).pin_memory()
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    wss = [ginf.Workspace(), ginf.Workspace()]
+    labs = [torch.zeros((110, 150), dtype=torch.int32).pin_memory() for _ in range(4)]
+    es = [ctypes.c_double() for _ in range(4)]
+    for access in (ginf.HOST_COPY, ginf.HOST_AUTO):
+        for i in range(4):
+            ginf.solve_async(D, V, P.model, 3, 6, 2, labs[i], es[i], wss[i % 2], streams[i % 2].cuda_stream,
+                             host_access=access)
+        for w in wss:
+            w.sync()
+        for i in range(4):
+            assert np.array_equal(labs[i].numpy()[1:-1, 1:-1], want_lab[1:-1, 1:-1]), (access, i)
+            assert es[i].value == want_e, (access, i)
+            labs[i].zero_()
+            es[i].value = 0.0
+    with pytest.raises(ginf.GinfError):   # no workspace
+        g = ginf.make_grid(P.D, P.V, P.model)
+        o = ginf.options(asynchronous=1)
+        lab = np.zeros((110, 150), np.int32)
+        ginf.check(ginf.lib().ginf_decode_hbp(None, ctypes.byref(g), 3, 6, lab.ctypes.data, ctypes.byref(o), None))
+    with pytest.raises(ginf.GinfError):   # stats requested
+        ginf.decode_hbp(P.D, P.V, P.model, 3, 6, workspace=wss[0], want_stats=True, asynchronous=1)
+    for w in wss:
+        w.close()
