@@ -40,7 +40,7 @@ class Grid(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("msg_rule", _i32), ("msg_store", _i32), ("decode", _i32), ("normalize", _i32),
                 ("compute_type", _i32), ("tile_nodes", _i32), ("sweeps_per_launch", _i32), ("autotune", _i32),
-                ("stream", _p), ("msgs_out", _p), ("host_access", _i32), ("asynchronous", _i32),
+                ("stream", _p), ("msgs_out", _p), ("host_access", _i32), ("stream_ordered", _i32),
                 ("reserved", ctypes.c_int64 * 5)]
 
 
@@ -197,7 +197,7 @@ def make_grid(D, V, model):
 
 def options(rule=RULE_REFERENCE, store=STORE_NATIVE, decode=DECODE_STALE, normalize=NORM_MEAN, compute_type=-1,
             tile_nodes=0, sweeps_per_launch=0, autotune=0, stream=None, msgs_out=None, host_access=0,
-            asynchronous=0):
+            stream_ordered=0):
     o = Options()
     lib().ginf_default_options(ctypes.byref(o))
     o.msg_rule, o.msg_store, o.decode, o.normalize = rule, store, decode, normalize
@@ -206,7 +206,7 @@ def options(rule=RULE_REFERENCE, store=STORE_NATIVE, decode=DECODE_STALE, normal
     o.stream = stream if stream is not None else None
     o.msgs_out = msgs_out
     o.host_access = host_access
-    o.asynchronous = asynchronous
+    o.stream_ordered = stream_ordered
     return o
 
 
@@ -283,7 +283,7 @@ def solve_async(D, V, model, levels, iters, icm_iters, labels, energy, workspace
     `energy` the FP64 energy once the stream (or workspace.sync()) is done;
     D, V, labels and energy must stay alive and unchanged until then."""
     g = make_grid(D, V, model)
-    o = options(stream=stream, asynchronous=1, **opt)
+    o = options(stream=stream, stream_ordered=1, **opt)
     check(lib().ginf_solve(workspace.handle, ctypes.byref(g), levels, iters, icm_iters, _ptr(labels)[0],
                            ctypes.byref(energy), ctypes.byref(o), None))
 

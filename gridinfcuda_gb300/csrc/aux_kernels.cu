@@ -183,21 +183,26 @@ __global__ void k_export(const unsigned char *__restrict__ rec, int W, int H, in
     dst[idx] = v;
 }
 
-// One ICM node update, grid.cc:127-136 and icm.cc:10-34: eight lanes per
-// node, lane g taking the 16-byte label chunks g, g+8, ...; the cost of label
-// l is D + V(l,f_S) + V(l,f_E) + V(l,f_N) + V(l,f_W) in that order, with V
-// staged in shared memory row by row (Vs[f*Lp + l] = V(l, f)).  The eight
-// partial first-minima are combined by (value, label), which reproduces the
-// sequential argmin with strict < (lowest label on ties).
-template <typename T>
-__device__ __forceinline__ int icm_node(const unsigned char *rec, int W, int L, int Lp, uint32_t rec_bytes,
-                                        const T *Vs, const int32_t *lab, int x, int y, int g, int *status) {
+// One ICM node update, grid.cc:127-136 and icm.cc:10-34: LANES lanes per
+// node, lane g taking the 16-byte label chunks g, g+LANES, ...; the cost of
+// label l is D + V(l,f_S) + V(l,f_E) + V(l,f_N) + V(l,f_W) in that order,
+// with V staged in shared memory row by row (Vs[f*Lp + l] = V(l, f)).  The
+// partial first-minima of the lanes are combined by (value, label), which
+// reproduces the sequential argmin with strict < (lowest label on ties).
+template <typename T, int LANES>
+__device__ __forceinline__ int icm_node(const T *D, int W, int L, int Lp, const T *Vs, const int32_t *lab, int x,
+                                        int y, int g, int *status) {
     constexpr int E = 16 / sizeof(T);
-    const T *D = reinterpret_cast<const T *>(rec + ((size_t)y * W + x) * rec_bytes);
+    // The first cost chunk is requested before the neighbour labels, whose
+    // values the table reads depend on; each later chunk one step ahead.
+    int c = g * E;
+    T dv[E];
+    if (c < L) IcmIO<T>::load(D + c, dv);
     int f[4];
 #pragma unroll
+    for (int d = 0; d < 4; ++d) f[d] = lab[(size_t)(y + ddy(d)) * W + (x + ddx(d))];
+#pragma unroll
     for (int d = 0; d < 4; ++d) {
-        f[d] = lab[(size_t)(y + ddy(d)) * W + (x + ddx(d))];
         if (f[d] < 0 || f[d] >= L) {
             if (status && g == 0) atomicOr(status, DEV_ERR_BOUNDS);
             f[d] = 0;
@@ -205,9 +210,10 @@ __device__ __forceinline__ int icm_node(const unsigned char *rec, int W, int L, 
     }
     T best = T(0);
     int bl = 0x7fffffff;
-    for (int c = g * E; c < L; c += 8 * E) {
-        T dv[E], v[4][E];
-        IcmIO<T>::load(D + c, dv);
+    for (; c < L; c += LANES * E) {
+        T dn[E], v[4][E];
+        const int cn = c + LANES * E;
+        if (cn < L) IcmIO<T>::load(D + cn, dn);
 #pragma unroll
         for (int d = 0; d < 4; ++d) IcmIO<T>::load(Vs + (size_t)f[d] * Lp + c, v[d]);
 #pragma unroll
@@ -223,9 +229,11 @@ __device__ __forceinline__ int icm_node(const unsigned char *rec, int W, int L, 
                 bl = i;
             }
         }
+#pragma unroll
+        for (int k = 0; k < E; ++k) dv[k] = dn[k];
     }
 #pragma unroll
-    for (int off = 1; off < 8; off <<= 1) {
+    for (int off = 1; off < LANES; off <<= 1) {
         const T ob = __shfl_xor_sync(0xffffffffu, best, off);
         const int ol = __shfl_xor_sync(0xffffffffu, bl, off);
         if (ol != 0x7fffffff && (bl == 0x7fffffff || ob < best || (!(best < ob) && ol < bl))) {
@@ -246,25 +254,50 @@ __device__ __forceinline__ void stage_table(const T *__restrict__ V, T *Vs, int 
     __syncthreads();
 }
 
-template <typename T>
-__global__ void k_icm_sync(const unsigned char *__restrict__ rec, int W, int H, int L, int Lp, uint32_t rec_bytes,
-                           const T *__restrict__ V, const int32_t *__restrict__ old_lab, int32_t *__restrict__ new_lab,
-                           int *status) {
+// Jacobi sweep over the interior nodes, LANES lanes per node: few lanes share
+// the per-node work (index, neighbour labels, the combine).  Two lanes suit
+// cost rows strided inside full BP records, four the packed cost-only
+// records.  I is the node-index type (32-bit whenever the node count allows).
+template <typename T, typename I, int LANES>
+__global__ void __launch_bounds__(kThreads, 6)
+    k_icm_sync(const unsigned char *__restrict__ rec, int W, int H, int L, int Lp, uint32_t rec_bytes,
+               const T *__restrict__ V, const int32_t *__restrict__ old_lab, int32_t *__restrict__ new_lab,
+               int *status) {
     extern __shared__ __align__(16) unsigned char icm_smem[];
     T *Vs = reinterpret_cast<T *>(icm_smem);
     stage_table(V, Vs, L, Lp);
-    const size_t n = (size_t)(W - 2) * (H - 2);
-    const int g = threadIdx.x & 7;
-    // Node groups are whole 8-lane slices of a warp, so every group either
-    // has a node or the whole slice skips it together.
-    for (size_t base = (size_t)blockIdx.x * (blockDim.x / 8); base < n; base += (size_t)gridDim.x * (blockDim.x / 8)) {
-        const size_t node = base + (threadIdx.x >> 3);
+    const I wi = (I)(W - 2);
+    const I n = wi * (I)(H - 2);
+    const int g = threadIdx.x & (LANES - 1);
+    constexpr int kPerBlock = kThreads / LANES;
+    // Node groups are whole lane slices of a warp, so every group either has
+    // a node or the whole slice skips it together.
+    for (I base = (I)blockIdx.x * kPerBlock; base < n; base += (I)gridDim.x * kPerBlock) {
+        const I node = base + (threadIdx.x / LANES);
         const bool act = node < n;
-        const size_t nn = act ? node : 0;
-        const int x = 1 + (int)(nn % (W - 2)), y = 1 + (int)(nn / (W - 2));
-        const int bl = icm_node<T>(rec, W, L, Lp, rec_bytes, Vs, old_lab, x, y, g, status);
+        const I nn = act ? node : 0;
+        const I row = nn / wi;
+        const int x = 1 + (int)(nn - row * wi), y = 1 + (int)row;
+        const T *D = reinterpret_cast<const T *>(rec + ((size_t)y * W + x) * rec_bytes);
+        const int bl = icm_node<T, LANES>(D, W, L, Lp, Vs, old_lab, x, y, g, status);
         if (act && g == 0) new_lab[(size_t)y * W + x] = bl;
     }
+}
+
+template <typename T, typename I, int LANES>
+cudaError_t launch_icm_sync_t(const RecordFormat &f, const unsigned char *rec, int W, int H, const void *V,
+                              const int32_t *old_labels, int32_t *new_labels, int *status, size_t blocks, size_t smem,
+                              cudaStream_t s) {
+    auto kern = k_icm_sync<T, I, LANES>;
+    static size_t configured = 48 * 1024;
+    if (smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    kern<<<(unsigned)blocks, kThreads, smem, s>>>(rec, W, H, f.L, f.Lp, f.rec_bytes, static_cast<const T *>(V),
+                                                   old_labels, new_labels, status);
+    return cudaGetLastError();
 }
 
 // Raster Gauss-Seidel (icm.cc:40-67) as an exact wavefront: on anti-diagonal
@@ -281,21 +314,24 @@ __global__ void k_icm_diag(const unsigned char *__restrict__ rec, int W, int H, 
     const int idx = blockIdx.x * (blockDim.x / 8) + (threadIdx.x >> 3);
     const bool act = ylo + idx <= yhi;
     const int y = act ? ylo + idx : ylo, x = s - y;
-    const int bl = icm_node<T>(rec, W, L, Lp, rec_bytes, Vs, lab, x, y, threadIdx.x & 7, status);
+    const T *D = reinterpret_cast<const T *>(rec + ((size_t)y * W + x) * rec_bytes);
+    const int bl = icm_node<T, 8>(D, W, L, Lp, Vs, lab, x, y, threadIdx.x & 7, status);
     if (act && (threadIdx.x & 7) == 0) lab[(size_t)y * W + x] = bl;
 }
 
 // Energy, grid.cc:102-125, in FP64: block partial sums over a fixed
 // grid-stride assignment, then one block adds the partials in a fixed tree,
 // so the result is identical from run to run.
-template <typename T>
+template <typename T, typename I>
 __global__ void k_energy_partial(const T *__restrict__ costs, size_t node_stride, size_t label_stride, int W, int H,
                                  int L, const T *__restrict__ V, const int32_t *__restrict__ f, double *partials,
                                  int *status) {
-    const size_t n = (size_t)(W - 2) * (H - 2);
+    const I wi = (I)(W - 2);
+    const I n = wi * (I)(H - 2);
     double acc = 0.0;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const int x = 1 + (int)(i % (W - 2)), y = 1 + (int)(i / (W - 2));
+    for (I i = (I)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (I)gridDim.x * blockDim.x) {
+        const I row = i / wi;
+        const int x = 1 + (int)(i - row * wi), y = 1 + (int)row;
         const int fl = f[(size_t)y * W + x];
         const int fn = f[(size_t)(y - 1) * W + x];
         const int fe = f[(size_t)y * W + x + 1];
@@ -581,16 +617,23 @@ cudaError_t launch_icm_sync(const RecordFormat &f, const unsigned char *rec, int
                             const int32_t *old_labels, int32_t *new_labels, int *status, cudaStream_t s) {
     if (W < 3 || H < 3) return cudaSuccess;
     const size_t n = (size_t)(W - 2) * (H - 2);
+    const bool packed = f.rec_bytes == f.d_bytes;
+    const size_t per_block = kThreads / (packed ? 4 : 2);
+    size_t blocks = (n + per_block - 1) / per_block;
+    const size_t cap = (size_t)num_sms() * 6;
+    if (blocks > cap) blocks = cap;
+    const bool narrow = n + blocks * per_block < 0xffffffffull;
     GINF_DISPATCH_T(f, {
         const size_t smem = (size_t)f.L * f.Lp * sizeof(T);
-        cudaError_t e = icm_smem_attr(k_icm_sync<T>, smem);
-        if (e != cudaSuccess) return e;
-        size_t blocks = (n + kThreads / 8 - 1) / (kThreads / 8);
-        const size_t cap = (size_t)num_sms() * 8;
-        if (blocks > cap) blocks = cap;
-        k_icm_sync<T><<<(unsigned)blocks, kThreads, smem, s>>>(rec, W, H, f.L, f.Lp, f.rec_bytes,
-                                                               static_cast<const T *>(V), old_labels, new_labels,
-                                                               status);
+        if (packed)
+            return narrow ? launch_icm_sync_t<T, uint32_t, 4>(f, rec, W, H, V, old_labels, new_labels, status, blocks,
+                                                              smem, s)
+                          : launch_icm_sync_t<T, size_t, 4>(f, rec, W, H, V, old_labels, new_labels, status, blocks,
+                                                            smem, s);
+        return narrow ? launch_icm_sync_t<T, uint32_t, 2>(f, rec, W, H, V, old_labels, new_labels, status, blocks, smem,
+                                                          s)
+                      : launch_icm_sync_t<T, size_t, 2>(f, rec, W, H, V, old_labels, new_labels, status, blocks, smem,
+                                                        s);
     })
     return cudaGetLastError();
 }
@@ -614,7 +657,7 @@ cudaError_t launch_icm_async_diag(const RecordFormat &f, const unsigned char *re
 int energy_num_partials(int W, int H) {
     const size_t n = (W > 2 && H > 2) ? (size_t)(W - 2) * (H - 2) : 0;
     size_t b = (n + kThreads - 1) / kThreads;
-    if (b > 2048) b = 2048;
+    if (b > 8192) b = 8192;
     if (b < 1) b = 1;
     return (int)b;
 }
@@ -627,9 +670,17 @@ cudaError_t launch_energy(int ctype, const void *costs, size_t node_stride, size
     }
     RecordFormat f;
     f.ctype = ctype;
-    GINF_DISPATCH_T(f, { k_energy_partial<T><<<num_partials, kThreads, 0, s>>>(
-                             static_cast<const T *>(costs), node_stride, label_stride, W, H, L,
-                             static_cast<const T *>(V), labels, partials, status); })
+    const bool narrow = (size_t)(W - 2) * (H - 2) + (size_t)num_partials * kThreads < 0xffffffffull;
+    GINF_DISPATCH_T(f, {
+        if (narrow)
+            k_energy_partial<T, uint32_t><<<num_partials, kThreads, 0, s>>>(
+                static_cast<const T *>(costs), node_stride, label_stride, W, H, L, static_cast<const T *>(V), labels,
+                partials, status);
+        else
+            k_energy_partial<T, size_t><<<num_partials, kThreads, 0, s>>>(
+                static_cast<const T *>(costs), node_stride, label_stride, W, H, L, static_cast<const T *>(V), labels,
+                partials, status);
+    })
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_energy_final<<<1, kThreads, 0, s>>>(partials, num_partials, out);

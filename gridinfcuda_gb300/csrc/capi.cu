@@ -245,7 +245,7 @@ ginf_status resolve(const ginf_grid *g, const ginf_options *o, Resolved &r) {
     if (o->host_access != GINF_HOST_AUTO && o->host_access != GINF_HOST_COPY)
         return fail(GINF_ERR_INVALID_ARGUMENT, "unknown host_access");
     r.host_access = o->host_access;
-    r.async = o->asynchronous != 0;
+    r.async = o->stream_ordered != 0;
     r.stream = static_cast<cudaStream_t>(o->stream);
     return GINF_OK;
 }

@@ -96,7 +96,7 @@ typedef struct ginf_options {
                                 pageable memory on systems with pageable access),
                                 fusing the transfer into the layout transform;
                                 GINF_HOST_COPY always stages them by a copy      */
-    int32_t asynchronous;    /* ginf_decode_hbp / ginf_solve: 1 = stream-ordered.
+    int32_t stream_ordered;  /* ginf_decode_hbp / ginf_solve: 1 = stream-ordered.
                                 The call enqueues its work on `stream` and returns;
                                 host outputs (labels, energy) are valid once the
                                 stream or ginf_workspace_sync(ws) has finished, and

@@ -301,10 +301,10 @@ def test_stream_ordered_solve(ginf):
             es[i].value = 0.0
     with pytest.raises(ginf.GinfError):   # no workspace
         g = ginf.make_grid(P.D, P.V, P.model)
-        o = ginf.options(asynchronous=1)
+        o = ginf.options(stream_ordered=1)
         lab = np.zeros((110, 150), np.int32)
         ginf.check(ginf.lib().ginf_decode_hbp(None, ctypes.byref(g), 3, 6, lab.ctypes.data, ctypes.byref(o), None))
     with pytest.raises(ginf.GinfError):   # stats requested
-        ginf.decode_hbp(P.D, P.V, P.model, 3, 6, workspace=wss[0], want_stats=True, asynchronous=1)
+        ginf.decode_hbp(P.D, P.V, P.model, 3, 6, workspace=wss[0], want_stats=True, stream_ordered=1)
     for w in wss:
         w.close()
