@@ -48,7 +48,7 @@ class Stats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in ("total_ms", "upload_ms", "prepare_ms", "sweep_ms", "level0_sweep_ms",
                                                "icm_ms", "energy_ms", "download_ms")] + \
                [(n, ctypes.c_int64) for n in ("kernel_launches", "level0_sweep_launches", "node_label_iters",
-                                              "h2d_bytes", "d2h_bytes", "warm_start_used")]
+                                              "h2d_bytes", "d2h_bytes", "warm_start_used", "level0_alg_bytes")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

@@ -38,6 +38,7 @@ cudaError_t launch_sweep(const RecordFormat &f, const SweepConfig &cfg, SweepPar
 }
 
 bool sweep_supported(const RecordFormat &f) { return f.L >= 2 && f.L <= kMaxLabels; }
+
 }  // namespace ginf_gpu
 
 namespace {
@@ -433,6 +434,13 @@ ginf_status table_radius(Call &c, Prepared &P, int &radius) {
     return GINF_OK;
 }
 
+// Bytes a half-sweep must move through HBM: per updated node its costs and
+// four incoming messages in, four outgoing messages out.
+int64_t sweep_alg_bytes(const RecordFormat &f, const Level &lv) {
+    const int64_t nodes = (int64_t)(lv.W - 2) * (lv.H - 2) / 2;
+    return nodes * ((int64_t)f.d_bytes + 8 * (int64_t)f.m_bytes);
+}
+
 // The HBP level loop on prepared records, levels `from` down to `to`:
 // bp.cc:121-166 (bp.cu:180-205).  Level `from` starts from zero messages at
 // the top of the pyramid, from the coarser level otherwise, or from the
@@ -507,7 +515,10 @@ ginf_status run_levels(Call &c, Prepared &P, int iters, int64_t &nli, int from, 
             p.write_labels = (t == 0 && stale && it >= iters - 2) ? 1 : 0;
             GINF_CK(launch_sweep(f, c.r.cfg, p, s, c.ws->num_sms));
             ++c.launches;
-            if (t == 0 && c.stats) ++c.stats->level0_sweep_launches;
+            if (t == 0 && c.stats) {
+                ++c.stats->level0_sweep_launches;
+                c.stats->level0_alg_bytes += sweep_alg_bytes(f, lv);
+            }
         }
         nli += (int64_t)lv.W * lv.H * f.L * iters;
     }

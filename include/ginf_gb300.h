@@ -124,6 +124,8 @@ typedef struct ginf_stats {
     int64_t node_label_iters; /* sum over levels of W_t*H_t*L*iterations       */
     int64_t h2d_bytes, d2h_bytes;
     int64_t warm_start_used;  /* learned solve: 1 = warm start kept, 0 = fell back */
+    int64_t level0_alg_bytes; /* HBM bytes the finest level's sweep launches must move by
+                                 their design (the roofline numerator)             */
 } ginf_stats;
 
 typedef struct ginf_workspace ginf_workspace;

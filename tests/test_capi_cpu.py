@@ -84,5 +84,5 @@ def test_default_options_layout(built_lib):
     assert (o.msg_rule, o.msg_store, o.decode, o.normalize, o.compute_type) == (0, 0, 0, 0, -1)
     assert ctypes.sizeof(capi.Options) == 8 * 4 + 2 * 8 + 6 * 8
     assert ctypes.sizeof(capi.Grid) == 6 * 4 + 2 * 8
-    assert ctypes.sizeof(capi.Stats) == 8 * 8 + 6 * 8
+    assert ctypes.sizeof(capi.Stats) == 8 * 8 + 7 * 8
     assert capi.version().startswith("gridinfcuda-gb300")
