@@ -189,18 +189,20 @@ __global__ void k_export(const unsigned char *__restrict__ rec, int W, int H, in
 // with V staged in shared memory row by row (Vs[f*Lp + l] = V(l, f)).  The
 // partial first-minima of the lanes are combined by (value, label), which
 // reproduces the sequential argmin with strict < (lowest label on ties).
+// need == false skips the work (no loads) but still takes part in the lane
+// combine, which every lane of the warp must reach.
 template <typename T, int LANES>
 __device__ __forceinline__ int icm_node(const T *D, int W, int L, int Lp, const T *Vs, const int32_t *lab, int x,
-                                        int y, int g, int *status) {
+                                        int y, int g, int *status, bool need = true) {
     constexpr int E = 16 / sizeof(T);
     // The first cost chunk is requested before the neighbour labels, whose
     // values the table reads depend on; each later chunk one step ahead.
-    int c = g * E;
+    int c = need ? g * E : L;
     T dv[E];
     if (c < L) IcmIO<T>::load(D + c, dv);
     int f[4];
 #pragma unroll
-    for (int d = 0; d < 4; ++d) f[d] = lab[(size_t)(y + ddy(d)) * W + (x + ddx(d))];
+    for (int d = 0; d < 4; ++d) f[d] = need ? lab[(size_t)(y + ddy(d)) * W + (x + ddx(d))] : 0;
 #pragma unroll
     for (int d = 0; d < 4; ++d) {
         if (f[d] < 0 || f[d] >= L) {
@@ -258,11 +260,15 @@ __device__ __forceinline__ void stage_table(const T *__restrict__ V, T *Vs, int 
 // the per-node work (index, neighbour labels, the combine).  Two lanes suit
 // cost rows strided inside full BP records, four the packed cost-only
 // records.  I is the node-index type (32-bit whenever the node count allows).
+// chg_in (NULL on the first sweep) flags the nodes the previous sweep
+// changed: a node none of whose four neighbours changed would compute the
+// same minimisation as last time, so it keeps its label without reading its
+// costs.  chg_out receives this sweep's flags (border entries stay 0).
 template <typename T, typename I, int LANES>
 __global__ void __launch_bounds__(kThreads, 6)
     k_icm_sync(const unsigned char *__restrict__ rec, int W, int H, int L, int Lp, uint32_t rec_bytes,
                const T *__restrict__ V, const int32_t *__restrict__ old_lab, int32_t *__restrict__ new_lab,
-               int *status) {
+               const uint8_t *__restrict__ chg_in, uint8_t *__restrict__ chg_out, int *status) {
     extern __shared__ __align__(16) unsigned char icm_smem[];
     T *Vs = reinterpret_cast<T *>(icm_smem);
     stage_table(V, Vs, L, Lp);
@@ -278,16 +284,23 @@ __global__ void __launch_bounds__(kThreads, 6)
         const I nn = act ? node : 0;
         const I row = nn / wi;
         const int x = 1 + (int)(nn - row * wi), y = 1 + (int)row;
-        const T *D = reinterpret_cast<const T *>(rec + ((size_t)y * W + x) * rec_bytes);
-        const int bl = icm_node<T, LANES>(D, W, L, Lp, Vs, old_lab, x, y, g, status);
-        if (act && g == 0) new_lab[(size_t)y * W + x] = bl;
+        const size_t i = (size_t)y * W + x;
+        const bool need = !chg_in || (chg_in[i - W] | chg_in[i + W] | chg_in[i - 1] | chg_in[i + 1]) != 0;
+        const T *D = reinterpret_cast<const T *>(rec + i * rec_bytes);
+        int bl = icm_node<T, LANES>(D, W, L, Lp, Vs, old_lab, x, y, g, status, need);
+        if (act && g == 0) {
+            const int prev = old_lab[i];
+            if (!need) bl = prev;
+            new_lab[i] = bl;
+            chg_out[i] = bl != prev ? 1 : 0;
+        }
     }
 }
 
 template <typename T, typename I, int LANES>
 cudaError_t launch_icm_sync_t(const RecordFormat &f, const unsigned char *rec, int W, int H, const void *V,
-                              const int32_t *old_labels, int32_t *new_labels, int *status, size_t blocks, size_t smem,
-                              cudaStream_t s) {
+                              const int32_t *old_labels, int32_t *new_labels, const uint8_t *chg_in, uint8_t *chg_out,
+                              int *status, size_t blocks, size_t smem, cudaStream_t s) {
     auto kern = k_icm_sync<T, I, LANES>;
     static size_t configured = 48 * 1024;
     if (smem > configured) {
@@ -296,7 +309,7 @@ cudaError_t launch_icm_sync_t(const RecordFormat &f, const unsigned char *rec, i
         configured = smem;
     }
     kern<<<(unsigned)blocks, kThreads, smem, s>>>(rec, W, H, f.L, f.Lp, f.rec_bytes, static_cast<const T *>(V),
-                                                   old_labels, new_labels, status);
+                                                   old_labels, new_labels, chg_in, chg_out, status);
     return cudaGetLastError();
 }
 
@@ -614,7 +627,8 @@ int num_sms() {
 }
 
 cudaError_t launch_icm_sync(const RecordFormat &f, const unsigned char *rec, int W, int H, const void *V,
-                            const int32_t *old_labels, int32_t *new_labels, int *status, cudaStream_t s) {
+                            const int32_t *old_labels, int32_t *new_labels, const uint8_t *chg_in, uint8_t *chg_out,
+                            int *status, cudaStream_t s) {
     if (W < 3 || H < 3) return cudaSuccess;
     const size_t n = (size_t)(W - 2) * (H - 2);
     const bool packed = f.rec_bytes == f.d_bytes;
@@ -626,14 +640,14 @@ cudaError_t launch_icm_sync(const RecordFormat &f, const unsigned char *rec, int
     GINF_DISPATCH_T(f, {
         const size_t smem = (size_t)f.L * f.Lp * sizeof(T);
         if (packed)
-            return narrow ? launch_icm_sync_t<T, uint32_t, 4>(f, rec, W, H, V, old_labels, new_labels, status, blocks,
-                                                              smem, s)
-                          : launch_icm_sync_t<T, size_t, 4>(f, rec, W, H, V, old_labels, new_labels, status, blocks,
-                                                            smem, s);
-        return narrow ? launch_icm_sync_t<T, uint32_t, 2>(f, rec, W, H, V, old_labels, new_labels, status, blocks, smem,
-                                                          s)
-                      : launch_icm_sync_t<T, size_t, 2>(f, rec, W, H, V, old_labels, new_labels, status, blocks, smem,
-                                                        s);
+            return narrow ? launch_icm_sync_t<T, uint32_t, 4>(f, rec, W, H, V, old_labels, new_labels, chg_in, chg_out,
+                                                              status, blocks, smem, s)
+                          : launch_icm_sync_t<T, size_t, 4>(f, rec, W, H, V, old_labels, new_labels, chg_in, chg_out,
+                                                            status, blocks, smem, s);
+        return narrow ? launch_icm_sync_t<T, uint32_t, 2>(f, rec, W, H, V, old_labels, new_labels, chg_in, chg_out,
+                                                          status, blocks, smem, s)
+                      : launch_icm_sync_t<T, size_t, 2>(f, rec, W, H, V, old_labels, new_labels, chg_in, chg_out,
+                                                        status, blocks, smem, s);
     })
     return cudaGetLastError();
 }

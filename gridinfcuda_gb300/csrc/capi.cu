@@ -300,6 +300,7 @@ struct Prepared {
     void *Vt = nullptr;            // table in the compute type
     int32_t *lab = nullptr;        // device labels (caller's or a copy)
     int32_t *lab2 = nullptr;       // second label buffer (ICM ping-pong)
+    uint8_t *chg = nullptr;        // ICM change flags, two W*H byte maps (ping-pong)
     double *partials = nullptr;    // energy partials, status word follows
     int num_partials = 0;
     int *status = nullptr;
@@ -350,6 +351,7 @@ ginf_status prepare(Call &c, Prepared &P, int levels, bool want_lab2, const int3
     const size_t id_t = a.add(table_t);
     const size_t id_lab = (labels_dev == nullptr) ? a.add(lab_bytes) : 0;
     const size_t id_lab2 = want_lab2 ? a.add(lab_bytes) : 0;
+    const size_t id_chg = want_lab2 ? a.add(2 * (size_t)W * H) : 0;
     const size_t id_part = a.add(sizeof(double) * (P.num_partials + 1) + 64);
     GINF_TRY(ws_reserve(c.ws, a.total()));
     unsigned char *base = c.ws->arena;
@@ -357,6 +359,7 @@ ginf_status prepare(Call &c, Prepared &P, int levels, bool want_lab2, const int3
     P.Vt = a.ptr(base, id_t);
     P.lab = labels_dev ? labels_dev : reinterpret_cast<int32_t *>(a.ptr(base, id_lab));
     P.lab2 = want_lab2 ? reinterpret_cast<int32_t *>(a.ptr(base, id_lab2)) : nullptr;
+    P.chg = want_lab2 ? a.ptr(base, id_chg) : nullptr;
     P.partials = reinterpret_cast<double *>(a.ptr(base, id_part));
     P.status = reinterpret_cast<int *>(P.partials + P.num_partials);
     P.energy = P.partials + P.num_partials + 1;
@@ -544,9 +547,14 @@ ginf_status run_icm_sync(Call &c, Prepared &P, int iters) {
     cudaStream_t s = c.r.stream;
     if (iters <= 0 || W < 3 || H < 3) return GINF_OK;
     GINF_CK(cudaMemcpyAsync(P.lab2, P.lab, lab_bytes, cudaMemcpyDeviceToDevice, s));
+    const size_t plane = (size_t)W * H;
+    GINF_CK(cudaMemsetAsync(P.chg, 0, 2 * plane, s));
     int32_t *src = P.lab, *dst = P.lab2;
     for (int it = 0; it < iters; ++it) {
-        GINF_CK(launch_icm_sync(P.f, P.rec, W, H, P.Vt, src, dst, P.status, s));
+        // Sweep it reads the flags sweep it-1 wrote (none on the first).
+        const uint8_t *chg_in = it == 0 ? nullptr : P.chg + ((it - 1) & 1) * plane;
+        uint8_t *chg_out = P.chg + (it & 1) * plane;
+        GINF_CK(launch_icm_sync(P.f, P.rec, W, H, P.Vt, src, dst, chg_in, chg_out, P.status, s));
         ++c.launches;
         std::swap(src, dst);
     }

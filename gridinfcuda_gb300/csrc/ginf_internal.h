@@ -91,7 +91,8 @@ cudaError_t launch_decode_fresh(const RecordFormat &f, const unsigned char *rec,
 cudaError_t launch_export_messages(const RecordFormat &f, const unsigned char *rec, int W, int H, void *dst,
                                    cudaStream_t s);
 cudaError_t launch_icm_sync(const RecordFormat &f, const unsigned char *rec, int W, int H, const void *V,
-                            const int32_t *old_labels, int32_t *new_labels, int *status, cudaStream_t s);
+                            const int32_t *old_labels, int32_t *new_labels, const uint8_t *chg_in, uint8_t *chg_out,
+                            int *status, cudaStream_t s);
 cudaError_t launch_icm_async_diag(const RecordFormat &f, const unsigned char *rec, int W, int H, const void *V,
                                   int32_t *labels, int diag, int *status, cudaStream_t s);
 // Energy with costs addressed as base + node*node_stride + label*label_stride
