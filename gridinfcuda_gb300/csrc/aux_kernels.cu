@@ -68,6 +68,53 @@ __global__ void k_costs_to_records(const Tin *__restrict__ src, int W, int H, in
     }
 }
 
+// The same transform for two level-0 rows (2Y, 2Y+1) per block, which also
+// writes the level-1 costs of the 16 coarse nodes those 32 columns cover:
+// each sum is formed from the transposed tiles in shared memory in the
+// order k_pyramid uses, so level 0 is not read back for level 1.
+template <typename Tin, typename T>
+__global__ void k_costs_to_records_pyr(const Tin *__restrict__ src, int W, int H, int L, int Lp,
+                                       unsigned char *__restrict__ rec, unsigned char *__restrict__ crec, int cW,
+                                       uint32_t rec_bytes) {
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    T *tile = reinterpret_cast<T *>(sm_raw);  // [2][Lp][33]
+    const int x0 = blockIdx.x * 32, Y = blockIdx.y;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int rows = min(2, H - 2 * Y);
+    for (int r = 0; r < rows; ++r) {
+        const int y = 2 * Y + r;
+        for (int l = ty; l < Lp; l += 8) {
+            const int x = x0 + tx;
+            T v = T(0);
+            if (l < L && x < W) v = (T)src[(size_t)x + (size_t)W * y + (size_t)W * H * l];
+            tile[(r * Lp + l) * 33 + tx] = v;
+        }
+    }
+    __syncthreads();
+    const int nn = min(32, W - x0);
+    for (int r = 0; r < rows; ++r) {
+        const int y = 2 * Y + r;
+        for (int idx = ty * 32 + tx; idx < nn * Lp; idx += 256) {
+            const int i = idx / Lp, l = idx - i * Lp;
+            T *d = reinterpret_cast<T *>(rec + ((size_t)y * W + x0 + i) * rec_bytes);
+            d[l] = tile[(r * Lp + l) * 33 + i];
+        }
+    }
+    const int cn = min(16, cW - x0 / 2);
+    for (int idx = ty * 32 + tx; idx < cn * Lp; idx += 256) {
+        const int i = idx / Lp, l = idx - i * Lp;
+        T acc = T(0);
+        if (l < L) {
+            for (int r = 0; r < rows; ++r)
+                for (int dx = 0; dx < 2; ++dx) {
+                    if (x0 + 2 * i + dx >= W) break;
+                    acc += tile[(r * Lp + l) * 33 + 2 * i + dx];
+                }
+        }
+        reinterpret_cast<T *>(crec + ((size_t)Y * cW + x0 / 2 + i) * rec_bytes)[l] = acc;
+    }
+}
+
 // HBP pyramid, bp.cc:100-117: D_t(X,Y) = sum of the (up to) four finer nodes,
 // accumulated from zero in the finer level's raster order.
 template <typename T>
@@ -556,6 +603,29 @@ cudaError_t launch_costs_to_records(const RecordFormat &f, int cost_type, const 
         else
             k_costs_to_records<int, T><<<grid, block, smem, s>>>(static_cast<const int *>(src), W, H, f.L, f.Lp, rec,
                                                                  f.rec_bytes);
+    })
+    return cudaGetLastError();
+}
+
+cudaError_t launch_costs_to_records_pyr(const RecordFormat &f, int cost_type, const void *src, int W, int H,
+                                        unsigned char *rec, unsigned char *crec, int cW, cudaStream_t s) {
+    const dim3 grid((W + 31) / 32, (H + 1) / 2), block(32, 8);
+    GINF_DISPATCH_T(f, {
+        const size_t smem = (size_t)2 * f.Lp * 33 * sizeof(T);
+        if (smem > 48 * 1024) {
+            cudaError_t e = cost_type == CT_F32
+                                ? cudaFuncSetAttribute(k_costs_to_records_pyr<float, T>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                                : cudaFuncSetAttribute(k_costs_to_records_pyr<int, T>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        if (cost_type == CT_F32)
+            k_costs_to_records_pyr<float, T><<<grid, block, smem, s>>>(static_cast<const float *>(src), W, H, f.L,
+                                                                       f.Lp, rec, crec, cW, f.rec_bytes);
+        else
+            k_costs_to_records_pyr<int, T><<<grid, block, smem, s>>>(static_cast<const int *>(src), W, H, f.L, f.Lp,
+                                                                     rec, crec, cW, f.rec_bytes);
     })
     return cudaGetLastError();
 }

@@ -396,9 +396,16 @@ ginf_status prepare(Call &c, Prepared &P, int levels, bool want_lab2, const int3
         GINF_CK(launch_convert_table(g->cost_type, c.r.ctype, table_dev, P.Vt, L * L, s));
         ++c.launches;
     }
-    GINF_CK(launch_costs_to_records(P.f, g->cost_type, costs_dev, W, H, P.rec, s));
+    // Level 0 records, with level 1's costs formed on the way when there is
+    // a pyramid; then the coarser levels.
+    const int nlv = (int)P.lv.size();
+    if (nlv >= 2)
+        GINF_CK(launch_costs_to_records_pyr(P.f, g->cost_type, costs_dev, W, H, P.rec, P.rec + P.lv[1].off,
+                                            P.lv[1].W, s));
+    else
+        GINF_CK(launch_costs_to_records(P.f, g->cost_type, costs_dev, W, H, P.rec, s));
     ++c.launches;
-    for (int t = 1; t < (int)P.lv.size(); ++t) {
+    for (int t = 2; t < nlv; ++t) {
         GINF_CK(launch_pyramid(P.f, P.rec + P.lv[t - 1].off, P.lv[t - 1].W, P.lv[t - 1].H, P.rec + P.lv[t].off,
                                P.lv[t].W, P.lv[t].H, s));
         ++c.launches;

@@ -81,6 +81,9 @@ bool sweep_supported(const RecordFormat &f);
 // Auxiliary kernels (aux_kernels.cu).
 cudaError_t launch_costs_to_records(const RecordFormat &f, int cost_type, const void *src, int W, int H,
                                     unsigned char *rec, cudaStream_t s);
+// The layout transform fused with the level-1 pyramid sums.
+cudaError_t launch_costs_to_records_pyr(const RecordFormat &f, int cost_type, const void *src, int W, int H,
+                                        unsigned char *rec, unsigned char *crec, int cW, cudaStream_t s);
 cudaError_t launch_pyramid(const RecordFormat &f, const unsigned char *frec, int fW, int fH, unsigned char *crec,
                            int cW, int cH, cudaStream_t s);
 cudaError_t launch_init_messages(const RecordFormat &f, unsigned char *rec, int W, int H,
