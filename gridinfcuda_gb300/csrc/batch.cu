@@ -1,5 +1,5 @@
 // batch.cu -- many independent grids solved together: one persistent,
-// cooperative launch walks a work list of (grid, tile) tickets for each
+// cooperative launch walks a work list of (grid, tile) entries for each
 // half-sweep, with a bounded grid barrier between half-sweeps; the whole
 // solve (layout transforms, initialisation, the persistent launches) is
 // captured once into a CUDA graph and replayed.  The tile shape and the
@@ -40,14 +40,25 @@ struct BatchLaunch {
     int count, total_tiles;
     int it_begin, it_end, iters;
     int first_mode;           // RD_ZERO (fused start) or RD_OWN (messages initialised)
-    unsigned int *tickets;    // one counter per half-sweep
     unsigned int *barrier;    // {arrived, generation}
     int *status;
+    uint32_t tile_smem;       // bytes of tile slots at the start of dynamic shared memory
+    int bases_in_smem;        // the grids' tile bases follow the slots
 };
 
-template <int NW>
-__device__ __forceinline__ bool batch_tile(const BatchLaunch &b, const BatchItem &g, int it, int t,
-                                           unsigned char *smem, uint64_t *bar, uint32_t &parity) {
+// Index of the grid that owns work-list tile t (tile bases ascending).
+__device__ __forceinline__ int batch_item_of(const BatchLaunch &b, const int *bases, int t) {
+    int lo = 0, hi = b.count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        const int base = bases ? bases[mid] : __ldg(&b.items[mid].tile_base);
+        if (base <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ SweepParams batch_params(const BatchLaunch &b, const BatchItem &g, int it) {
     SweepParams p{};
     p.W = g.W;
     p.H = g.H;
@@ -67,54 +78,54 @@ __device__ __forceinline__ bool batch_tile(const BatchLaunch &b, const BatchItem
     p.tiles_per_row = g.tiles_per_row;
     p.num_tiles = g.num_tiles;
     p.status = b.status;
-    tile_load<NW>(p, t, smem, bar);
-    switch (g.L) {
-        case 16:
-            return tile_finish<float, float, 16, true, NW, KIND_LINEAR>(p, table_consts<float, KIND_LINEAR>(g.V, 16),
-                                                                        t, smem, bar, parity);
-        case 32:
-            return tile_finish<float, float, 32, true, NW, KIND_LINEAR>(p, table_consts<float, KIND_LINEAR>(g.V, 32),
-                                                                        t, smem, bar, parity);
-        case 64:
-            return tile_finish<float, float, 64, true, NW, KIND_LINEAR>(p, table_consts<float, KIND_LINEAR>(g.V, 64),
-                                                                        t, smem, bar, parity);
-        default:
-            return tile_finish<float, float, 64, false, NW, KIND_LINEAR>(
-                p, table_consts<float, KIND_LINEAR>(g.V, g.L), t, smem, bar, parity);
-    }
+    return p;
 }
 
-// Persistent kernel: half-sweeps it_begin..it_end-1 of every grid.  Blocks
-// take tickets from the half-sweep's counter until the work list is done,
-// then meet at the grid barrier; before it each block waits for its own bulk
-// stores to complete and fences them against the next half-sweep's bulk
-// loads (issued by any block after the barrier).
-template <int NW>
+
+// Persistent kernel: half-sweeps it_begin..it_end-1 of every grid of one
+// label bucket (L == LM when EXACT, else L < LM; one kernel per bucket keeps
+// the register allocation of the single-grid sweep).  Within
+// a half-sweep the tiles of all grids are independent: block k takes work-
+// list tiles k, k + gridDim.x, ... and issues the bulk load of its next tile
+// as soon as the current one is done (the grid owning a tile is found by a
+// binary search over the tile bases, kept in shared memory).  Between
+// half-sweeps each block waits for its own bulk stores, fences them against
+// the next half-sweep's bulk loads and meets the others at the grid barrier.
+template <int NW, int LM, bool EXACT>
 __global__ void __launch_bounds__(NW * 32) batch_kernel(const BatchLaunch b) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t full_bar;
-    __shared__ int s_ticket;
+    int *bases_s = reinterpret_cast<int *>(smem + b.tile_smem);
     if (threadIdx.x == 0) {
         mbar_init(&full_bar, NW * 32);
         fence_barrier_init();
     }
+    if (b.bases_in_smem)
+        for (int i = threadIdx.x; i < b.count; i += blockDim.x) bases_s[i] = b.items[i].tile_base;
     __syncthreads();
+    const int *bases = b.bases_in_smem ? bases_s : nullptr;
     uint32_t parity = 0;
     for (int it = b.it_begin; it < b.it_end; ++it) {
-        for (;;) {
-            if (threadIdx.x == 0) s_ticket = (int)atomicAdd(&b.tickets[it], 1u);
-            __syncthreads();
-            const int ticket = s_ticket;
-            __syncthreads();
-            if (ticket >= b.total_tiles) break;
-            int lo = 0, hi = b.count - 1;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (b.items[mid].tile_base <= ticket) lo = mid;
-                else hi = mid - 1;
+        int t = blockIdx.x;
+        SweepParams p{};
+        int base = 0;
+        if (t < b.total_tiles) {
+            const BatchItem &g = b.items[batch_item_of(b, bases, t)];
+            p = batch_params(b, g, it);
+            base = g.tile_base;
+            tile_load<NW>(p, t - base, smem, &full_bar);
+        }
+        for (; t < b.total_tiles; t += gridDim.x) {
+            if (!tile_finish<float, float, LM, EXACT, NW, KIND_LINEAR>(
+                    p, table_consts<float, KIND_LINEAR>(p.V, EXACT ? LM : p.L), t - base, smem, &full_bar, parity))
+                return;
+            const int tn = t + gridDim.x;
+            if (tn < b.total_tiles) {
+                const BatchItem &g = b.items[batch_item_of(b, bases, tn)];
+                p = batch_params(b, g, it);
+                base = g.tile_base;
+                tile_load<NW>(p, tn - base, smem, &full_bar);
             }
-            const BatchItem g = b.items[lo];
-            if (!batch_tile<NW>(b, g, it, ticket - g.tile_base, smem, &full_bar, parity)) return;
         }
         bulk_wait_all();
         fence_proxy_async_global();
@@ -233,6 +244,16 @@ ginf_status bfail(ginf_status s, const std::string &msg) {
 
 }  // namespace
 
+// Grids whose label count falls in one bucket (LM = 16, 32 or 64; exact when
+// L == LM), solved by one kernel instantiation; items first..first+count-1.
+struct BatchGroup {
+    int lm = 64;
+    bool exact = true;
+    int first = 0, count = 0;
+    int total_tiles = 0;
+    uint32_t max_slot = 0;
+};
+
 struct ginf_batch {
     int count = 0, iters = 0;
     std::vector<ginf_grid> grids;
@@ -241,13 +262,14 @@ struct ginf_batch {
     unsigned char *arena = nullptr;
     size_t arena_bytes = 0;
     BatchItem *items_dev = nullptr;
-    unsigned int *tickets = nullptr;
     unsigned int *barrier = nullptr;
     int *status = nullptr;
     int *status_host = nullptr;
     std::vector<unsigned char *> rec;
     int num_sms = 0;
     uint32_t max_slot = 0;
+    std::vector<BatchGroup> groups;  // grids by label bucket, in items order
+    std::vector<int> order;          // grid index of each item
     TuneChoice choice;
     int launches_per_run = 0;
     cudaStream_t cap_stream = nullptr;
@@ -259,38 +281,68 @@ struct ginf_batch {
 
 namespace {
 
-// Items for a given tile size (8 * NW nodes); copied to the device.
-std::vector<BatchItem> make_items(ginf_batch *b, int tile_nodes, int &total_tiles) {
+int label_bucket(int L) { return L <= 16 ? 16 : (L <= 32 ? 32 : 64); }
+
+// Groups the grids by label bucket (once, at creation).
+void make_groups(ginf_batch *b) {
+    b->groups.clear();
+    b->order.clear();
+    for (int lm : {16, 32, 64})
+        for (int exact = 1; exact >= 0; --exact) {
+            BatchGroup grp;
+            grp.lm = lm;
+            grp.exact = exact != 0;
+            grp.first = (int)b->order.size();
+            for (int i = 0; i < b->count; ++i) {
+                const int L = b->grids[i].num_labels;
+                if (label_bucket(L) != lm || (L == lm) != grp.exact) continue;
+                b->order.push_back(i);
+                grp.max_slot = std::max(grp.max_slot, b->fmt[i].slot_bytes);
+            }
+            grp.count = (int)b->order.size() - grp.first;
+            if (grp.count > 0) b->groups.push_back(grp);
+        }
+}
+
+// Items for a given tile size (8 * NW nodes), in group order, with tile
+// bases counted from each group's start; copied to the device.
+std::vector<BatchItem> make_items(ginf_batch *b, int tile_nodes) {
     std::vector<BatchItem> items(b->count);
-    total_tiles = 0;
-    for (int i = 0; i < b->count; ++i) {
-        const ginf_grid &g = b->grids[i];
-        const RecordFormat &f = b->fmt[i];
-        BatchItem &it = items[i];
-        it.rec = b->rec[i];
-        it.labels = b->labels[i];
-        it.V = static_cast<const float *>(g.sm_costs);
-        it.W = g.width;
-        it.H = g.height;
-        it.L = g.num_labels;
-        it.Lp = f.Lp;
-        it.rec_bytes = f.rec_bytes;
-        it.d_bytes = f.d_bytes;
-        it.m_bytes = f.m_bytes;
-        it.slot_bytes = f.slot_bytes;
-        const int n1 = g.width >= 3 ? (g.width - 3) / 2 + 1 : 0;
-        it.tiles_per_row = (n1 + tile_nodes - 1) / tile_nodes;
-        it.num_tiles = (g.width >= 3 && g.height >= 3) ? (g.height - 2) * it.tiles_per_row : 0;
-        it.tile_base = total_tiles;
-        total_tiles += it.num_tiles;
+    for (auto &grp : b->groups) {
+        grp.total_tiles = 0;
+        for (int k = grp.first; k < grp.first + grp.count; ++k) {
+            const int i = b->order[k];
+            const ginf_grid &g = b->grids[i];
+            const RecordFormat &f = b->fmt[i];
+            BatchItem &it = items[k];
+            it.rec = b->rec[i];
+            it.labels = b->labels[i];
+            it.V = static_cast<const float *>(g.sm_costs);
+            it.W = g.width;
+            it.H = g.height;
+            it.L = g.num_labels;
+            it.Lp = f.Lp;
+            it.rec_bytes = f.rec_bytes;
+            it.d_bytes = f.d_bytes;
+            it.m_bytes = f.m_bytes;
+            it.slot_bytes = f.slot_bytes;
+            const int n1 = g.width >= 3 ? (g.width - 3) / 2 + 1 : 0;
+            it.tiles_per_row = (n1 + tile_nodes - 1) / tile_nodes;
+            it.num_tiles = (g.width >= 3 && g.height >= 3) ? (g.height - 2) * it.tiles_per_row : 0;
+            it.tile_base = grp.total_tiles;
+            grp.total_tiles += it.num_tiles;
+        }
     }
     return items;
 }
 
-template <int NW>
-cudaError_t launch_batch(const BatchLaunch &bl, uint32_t max_slot, int num_sms, cudaStream_t s) {
-    auto kern = batch_kernel<NW>;
-    const size_t smem = (size_t)NW * 8 * max_slot;
+template <int NW, int LM, bool EXACT>
+cudaError_t launch_batch(BatchLaunch bl, uint32_t max_slot, int num_sms, cudaStream_t s) {
+    auto kern = batch_kernel<NW, LM, EXACT>;
+    bl.tile_smem = (uint32_t)(((size_t)NW * 8 * max_slot + 15) / 16 * 16);
+    const size_t bases_bytes = sizeof(int) * (size_t)bl.count;
+    bl.bases_in_smem = bases_bytes <= 16 * 1024 ? 1 : 0;
+    const size_t smem = bl.tile_smem + (bl.bases_in_smem ? bases_bytes : 0);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int occ = 0;
@@ -312,12 +364,29 @@ cudaError_t launch_batch(const BatchLaunch &bl, uint32_t max_slot, int num_sms, 
     return cudaLaunchKernelEx(&cfg, kern, bl);
 }
 
+template <int LM, bool EXACT>
+cudaError_t launch_batch_nw(int tile_nodes, const BatchLaunch &bl, uint32_t max_slot, int num_sms, cudaStream_t s) {
+    if (tile_nodes == 8) return launch_batch<1, LM, EXACT>(bl, max_slot, num_sms, s);
+    if (tile_nodes == 32) return launch_batch<4, LM, EXACT>(bl, max_slot, num_sms, s);
+    return launch_batch<2, LM, EXACT>(bl, max_slot, num_sms, s);
+}
+
+cudaError_t launch_group(const BatchGroup &grp, int tile_nodes, const BatchLaunch &bl, int num_sms, cudaStream_t s) {
+    switch (grp.lm * 2 + (grp.exact ? 1 : 0)) {
+        case 33: return launch_batch_nw<16, true>(tile_nodes, bl, grp.max_slot, num_sms, s);
+        case 32: return launch_batch_nw<16, false>(tile_nodes, bl, grp.max_slot, num_sms, s);
+        case 65: return launch_batch_nw<32, true>(tile_nodes, bl, grp.max_slot, num_sms, s);
+        case 64: return launch_batch_nw<32, false>(tile_nodes, bl, grp.max_slot, num_sms, s);
+        case 129: return launch_batch_nw<64, true>(tile_nodes, bl, grp.max_slot, num_sms, s);
+        default: return launch_batch_nw<64, false>(tile_nodes, bl, grp.max_slot, num_sms, s);
+    }
+}
+
 // Records the whole batch solve on stream s: layout transforms, start-up
-// initialisation, counters, persistent launches.
+// initialisation, counters, then per label group its persistent launches.
 ginf_status record_solve(ginf_batch *b, const TuneChoice &c, cudaStream_t s, int &launches) {
     launches = 0;
-    int total_tiles = 0;
-    make_items(b, c.tile_nodes, total_tiles);  // the device copy was made before the capture
+    make_items(b, c.tile_nodes);  // the device copy was made before the capture
     const bool fused = b->iters >= 2;
     for (int i = 0; i < b->count; ++i) {
         const ginf_grid &g = b->grids[i];
@@ -329,32 +398,30 @@ ginf_status record_solve(ginf_batch *b, const TuneChoice &c, cudaStream_t s, int
             launches += 2;
         }
     }
-    GINF_BCK(cudaMemsetAsync(b->tickets, 0, sizeof(unsigned int) * (size_t)std::max(1, b->iters), s));
     GINF_BCK(cudaMemsetAsync(b->barrier, 0, 2 * sizeof(unsigned int), s));
     GINF_BCK(cudaMemsetAsync(b->status, 0, sizeof(int), s));
-    if (total_tiles == 0 || b->iters == 0) return GINF_OK;
+    if (b->iters == 0) return GINF_OK;
     const int spl = c.sweeps_per_launch <= 0 ? b->iters : std::min(c.sweeps_per_launch, b->iters);
-    for (int it0 = 0; it0 < b->iters; it0 += spl) {
-        BatchLaunch bl;
-        bl.items = b->items_dev;
-        bl.count = b->count;
-        bl.total_tiles = total_tiles;
-        bl.it_begin = it0;
-        bl.it_end = std::min(b->iters, it0 + spl);
-        bl.iters = b->iters;
-        bl.first_mode = fused ? RD_ZERO : RD_OWN;
-        bl.tickets = b->tickets;
-        bl.barrier = b->barrier;
-        bl.status = b->status;
-        cudaError_t e;
-        if (c.tile_nodes == 8) e = launch_batch<1>(bl, b->max_slot, b->num_sms, s);
-        else if (c.tile_nodes == 32) e = launch_batch<4>(bl, b->max_slot, b->num_sms, s);
-        else e = launch_batch<2>(bl, b->max_slot, b->num_sms, s);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            return bfail(GINF_ERR_CUDA, std::string("persistent batch launch: ") + cudaGetErrorString(e));
+    for (const BatchGroup &grp : b->groups) {
+        if (grp.total_tiles == 0) continue;
+        for (int it0 = 0; it0 < b->iters; it0 += spl) {
+            BatchLaunch bl{};
+            bl.items = b->items_dev + grp.first;
+            bl.count = grp.count;
+            bl.total_tiles = grp.total_tiles;
+            bl.it_begin = it0;
+            bl.it_end = std::min(b->iters, it0 + spl);
+            bl.iters = b->iters;
+            bl.first_mode = fused ? RD_ZERO : RD_OWN;
+            bl.barrier = b->barrier;
+            bl.status = b->status;
+            const cudaError_t e = launch_group(grp, c.tile_nodes, bl, b->num_sms, s);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                return bfail(GINF_ERR_CUDA, std::string("persistent batch launch: ") + cudaGetErrorString(e));
+            }
+            ++launches;
         }
-        ++launches;
     }
     return GINF_OK;
 }
@@ -371,8 +438,7 @@ void drop_graph(ginf_batch *b) {
 // here, before the capture, and the graph reads them from there.
 ginf_status capture(ginf_batch *b, const TuneChoice &c) {
     drop_graph(b);
-    int total_tiles = 0;
-    const std::vector<BatchItem> items = make_items(b, c.tile_nodes, total_tiles);
+    const std::vector<BatchItem> items = make_items(b, c.tile_nodes);
     GINF_BCK(cudaMemcpy(b->items_dev, items.data(), sizeof(BatchItem) * items.size(), cudaMemcpyHostToDevice));
     GINF_BCK(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal));
     int launches = 0;
@@ -494,7 +560,7 @@ ginf_status ginf_batch_create(ginf_batch **out, const ginf_grid *grids, int32_t 
     const size_t items_off = total;
     total += ((sizeof(BatchItem) * count + 255) / 256) * 256;
     const size_t ctl_off = total;
-    total += 256 + sizeof(unsigned int) * (size_t)std::max(1, iters);
+    total += 256;
     cudaError_t e = cudaMalloc(&b->arena, total);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -503,10 +569,10 @@ ginf_status ginf_batch_create(ginf_batch **out, const ginf_grid *grids, int32_t 
     }
     b->arena_bytes = total;
     for (int i = 0; i < count; ++i) b->rec.push_back(b->arena + off[i]);
+    make_groups(b);
     b->items_dev = reinterpret_cast<BatchItem *>(b->arena + items_off);
     b->barrier = reinterpret_cast<unsigned int *>(b->arena + ctl_off);
     b->status = reinterpret_cast<int *>(b->arena + ctl_off + 64);
-    b->tickets = reinterpret_cast<unsigned int *>(b->arena + ctl_off + 256);
     ginf_status st = GINF_OK;
     if (cudaMallocHost(&b->status_host, sizeof(int)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess ||
