@@ -103,6 +103,13 @@ __device__ __forceinline__ void fence_proxy_async_global() {
     asm volatile("fence.proxy.async.global;" ::: "memory");
 }
 
+// Programmatic dependent launch: the next kernel in the stream (launched
+// with programmatic stream serialisation) may start now; it waits in
+// grid_dependency_wait() until this grid has completed and its memory
+// operations are visible.
+__device__ __forceinline__ void launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Grid-wide barrier for a cooperative launch (all blocks co-resident).  bar
 // holds {arrived, generation}, zeroed before the launch.  The last block to
 // arrive resets the count and advances the generation; the others wait for

@@ -689,12 +689,17 @@ template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND>
 __global__ void __launch_bounds__(NW * 32) sweep_kernel(const SweepParams p) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t full_bar;
+    // The next half-sweep may be launched now; its blocks take SM slots as
+    // these retire and wait below before touching any record.
+    launch_dependents();
     const TableConsts<T> tc = table_consts<T, KIND>(p.V, EXACT ? LMAX : p.L);
     if (threadIdx.x == 0) {
         mbar_init(&full_bar, NW * 32);
         fence_barrier_init();
     }
     __syncthreads();
+    // Records (and labels) are written by the previous kernel in the stream.
+    grid_dependency_wait();
     int t = blockIdx.x;
     if (t < p.num_tiles) tile_load<NW>(p, t, smem, &full_bar);
     uint32_t parity = 0;
@@ -735,8 +740,20 @@ cudaError_t launch_one(const SweepParams &params, uint32_t slot_bytes, cudaStrea
     if (occ < 1) return cudaErrorInvalidConfiguration;
     int grid = occ * num_sms;
     if (grid > p.num_tiles) grid = p.num_tiles;
-    kern<<<grid, NW * 32, smem, s>>>(p);
-    return cudaGetLastError();
+    // Programmatic stream serialisation: this launch may begin while the
+    // previous kernel of the stream finishes (the kernel waits for it before
+    // reading records).
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(grid);
+    lc.blockDim = dim3(NW * 32);
+    lc.dynamicSmemBytes = smem;
+    lc.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    return cudaLaunchKernelEx(&lc, kern, p);
 }
 
 template <typename T, typename M, int LM>
