@@ -10,8 +10,10 @@ from gridinfcuda_gb300 import synth
 
 pytestmark = pytest.mark.gpu
 
+# Every label bucket of the batch kernels: exact 16 / 32 / 64 and the
+# non-exact ones below each (5, 24, 48).
 SHAPES = [(37, 29, 16), (64, 40, 32), (23, 61, 64), (50, 50, 24), (3, 7, 16), (129, 17, 16), (8, 3, 32),
-          (70, 45, 64)]
+          (70, 45, 64), (33, 21, 5), (41, 30, 48)]
 
 
 def _problems(seed0=0):
