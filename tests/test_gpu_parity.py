@@ -308,3 +308,26 @@ def test_stream_ordered_solve(ginf):
         ginf.decode_hbp(P.D, P.V, P.model, 3, 6, workspace=wss[0], want_stats=True, stream_ordered=1)
     for w in wss:
         w.close()
+
+
+@pytest.mark.parametrize("W,H", [(1, 1), (2, 9), (9, 2), (1, 40), (3, 3), (4, 3)])
+def test_grids_without_or_with_tiny_interior(ginf, orc, W, H):
+    """Grids with no interior node (nothing updates: every label stays the
+    caller's) or a one-node-wide interior, through BP, HBP, ICM, solve and the
+    energy, host and device buffers: equal to the oracle."""
+    import torch
+    P = synth.random_problem(W, H, 6, W * 17 + H)
+    init = (np.arange(W * H, dtype=np.int32).reshape(H, W) % 6).astype(np.int32)
+    for levels in (1, 3):
+        got = ginf.decode_hbp(P.D, P.V, P.model, levels, 4, labels=init.copy())
+        ref, _ = orc.hbp(P.D, P.V, P.model, levels, 4, want_msgs=True)
+        if W < 3 or H < 3:
+            assert np.array_equal(got, init), (levels, "no interior: labels unchanged")
+        else:
+            assert np.array_equal(got[1:-1, 1:-1], ref[1:-1, 1:-1]), levels
+        gd = ginf.decode_hbp(_dev(P.D), _dev(P.V), P.model, levels, 4, labels=_dev(init.copy())).cpu().numpy()
+        assert np.array_equal(gd, got), levels
+    icm = ginf.decode_icm(P.D, P.V, P.model, init, 3)
+    assert np.array_equal(icm, orc.icm(P.D, P.V, init, 3))
+    lab, e = ginf.solve(P.D, P.V, P.model, 2, 4, 2, labels=init.copy())
+    assert e == pytest.approx(orc.energy(P.D, P.V, lab), rel=1e-12, abs=1e-12)
