@@ -481,7 +481,7 @@ def run_batch(args, cfg):
         nli += W * H * L * cfg["iters"]
     t0 = time.perf_counter()
     plan = capi.Batch(problems, labels, cfg["iters"], autotune=1 if args.retune else 0,
-                      tile_nodes=args.tile_nodes)
+                      tile_nodes=args.tile_nodes, sweeps_per_launch=args.sweeps_per_launch)
     plan_s = time.perf_counter() - t0
     stream = torch.cuda.current_stream()
     for _ in range(args.warmup):
@@ -618,6 +618,8 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3, help="warm workload: Adam learning rate")
     ap.add_argument("--verbose", action="store_true")
     ap.add_argument("--retune", action="store_true", help="batch workload: re-measure the autotuner's choice")
+    ap.add_argument("--sweeps-per-launch", type=int, default=0,
+                    help="batch workload: half-sweeps per persistent launch (0: autotuned, with --tile-nodes 0)")
     ap.add_argument("--size", default=None, help="WxH override of the workload's grid size (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
