@@ -32,6 +32,7 @@ import argparse
 import ctypes
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -199,15 +200,41 @@ def cpu_port_step(P, cfg, nthreads):
     return oracle.energy(P.D, P.V, lab)
 
 
+def host_description():
+    """CPU model and core count of this host."""
+    model = platform.processor() or platform.machine()
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    return {"cpu_model": model, "nproc": os.cpu_count()}
+
+
 def cpu_baseline(P, cfg, nthreads):
+    """The oracle (C restatement of the reference algorithm) on the host: one
+    full step on all threads, and a single-core sample (the reference itself
+    is single-threaded): two half-sweeps of the finest level alone."""
     import oracle
     oracle.build()
     t0 = time.perf_counter()
     cpu_port_step(P, cfg, nthreads)
     dt = time.perf_counter() - t0
-    return {"value": nli_per_step(cfg) / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"one full step ({cfg['name']}) of the oracle C restatement, {nthreads} OpenMP threads, "
-                      f"{dt:.2f} s"}
+    t0 = time.perf_counter()
+    oracle.hbp(P.D, P.V, P.model, 1, 2, nthreads=1)
+    dt1 = time.perf_counter() - t0
+    nli1 = cfg["W"] * cfg["H"] * cfg["L"] * 2
+    out = {"value": nli_per_step(cfg) / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+           "sample": f"one full step ({cfg['name']}) of the oracle C restatement, {nthreads} OpenMP threads, "
+                     f"{dt:.2f} s",
+           "single_core": {"value": nli1 / dt1, "unit": UNIT, "cores": 1,
+                           "sample": f"2 half-sweeps of the {cfg['W']}x{cfg['H']}x{cfg['L']} finest level, "
+                                     f"1 thread, {dt1:.2f} s"}}
+    out.update(host_description())
+    return out
 
 
 # ---------------------------------------------------------------- our arm
@@ -524,8 +551,31 @@ def run_batch(args, cfg):
                 "e2e": {"value": world * args.steps * nli / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_s * 1e3 / args.steps, 3)},
                 "clocks": clock_info, "gpu_launches": int(sum(s["kernel_launches"] for s in sts))}
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = batch_cpu_baseline(problems, cfg["iters"])
         print(json.dumps(line), flush=True)
     plan.close()
+
+
+def batch_cpu_baseline(problems, iters, sample=8):
+    """Independent grids on all host cores: the oracle's BP (reference
+    semantics) on the first `sample` grids of the batch, OpenMP over rows."""
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    nli, dt = 0, 0.0
+    for D, V, model in problems[:sample]:
+        Dh, Vh = D.cpu().numpy(), V.cpu().numpy()
+        L, H, W = Dh.shape
+        t0 = time.perf_counter()
+        oracle.hbp(Dh, Vh, model, 1, iters, nthreads=threads)
+        dt += time.perf_counter() - t0
+        nli += W * H * L * iters
+    out = {"value": nli / dt, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"the first {sample} grids of the batch, {iters} half-sweeps each, {threads} OpenMP threads, "
+                     f"{dt:.2f} s"}
+    out.update(host_description())
+    return out
 
 
 # ---------------------------------------------------------------- learned warm start

@@ -32,7 +32,7 @@ struct BatchItem {
     int W, H, L, Lp;
     uint32_t rec_bytes, d_bytes, m_bytes, slot_bytes;
     int tiles_per_row, num_tiles;  // per half-sweep, for the launch's tile size
-    int tile_base;                 // first ticket of this grid
+    int tile_base;                 // first work-list tile of this grid (within its group)
 };
 
 struct BatchLaunch {
