@@ -51,20 +51,29 @@ __global__ void k_costs_to_records(const Tin *__restrict__ src, int W, int H, in
                                    unsigned char *__restrict__ rec, uint32_t rec_bytes) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     T *tile = reinterpret_cast<T *>(sm_raw);
-    const int x0 = blockIdx.x * 32, y = blockIdx.y;
+    const int x0 = blockIdx.x * 32;
     const int tx = threadIdx.x, ty = threadIdx.y;
-    for (int l = ty; l < Lp; l += 8) {
-        const int x = x0 + tx;
-        T v = T(0);
-        if (l < L && x < W) v = (T)src[(size_t)x + (size_t)W * y + (size_t)W * H * l];
-        tile[l * 33 + tx] = v;
-    }
-    __syncthreads();
+    // 16-byte chunks of consecutive labels (Lp is a multiple of 8).
+    constexpr int E = 16 / sizeof(T);
+    const int cpn = Lp / E;
     const int nn = min(32, W - x0);
-    for (int idx = ty * 32 + tx; idx < nn * Lp; idx += 256) {
-        const int i = idx / Lp, l = idx - i * Lp;
-        T *d = reinterpret_cast<T *>(rec + ((size_t)y * W + x0 + i) * rec_bytes);
-        d[l] = tile[l * 33 + i];
+    for (int y = blockIdx.y; y < H; y += gridDim.y) {
+        for (int l = ty; l < Lp; l += 8) {
+            const int x = x0 + tx;
+            T v = T(0);
+            if (l < L && x < W) v = (T)src[(size_t)x + (size_t)W * y + (size_t)W * H * l];
+            tile[l * 33 + tx] = v;
+        }
+        __syncthreads();
+        for (int q = ty * 32 + tx; q < nn * cpn; q += 256) {
+            const int i = q / cpn, l0 = (q - i * cpn) * E;
+            alignas(16) T v[E];
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = tile[(l0 + e) * 33 + i];
+            *reinterpret_cast<uint4 *>(rec + ((size_t)y * W + x0 + i) * rec_bytes + (size_t)l0 * sizeof(T)) =
+                *reinterpret_cast<const uint4 *>(v);
+        }
+        __syncthreads();
     }
 }
 
@@ -78,8 +87,10 @@ __global__ void k_costs_to_records_pyr(const Tin *__restrict__ src, int W, int H
                                        uint32_t rec_bytes) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     T *tile = reinterpret_cast<T *>(sm_raw);  // [2][Lp][33]
-    const int x0 = blockIdx.x * 32, Y = blockIdx.y;
+    const int x0 = blockIdx.x * 32;
     const int tx = threadIdx.x, ty = threadIdx.y;
+    const int cH = (H + 1) / 2;
+    for (int Y = blockIdx.y; Y < cH; Y += gridDim.y) {
     const int rows = min(2, H - 2 * Y);
     for (int r = 0; r < rows; ++r) {
         const int y = 2 * Y + r;
@@ -91,27 +102,39 @@ __global__ void k_costs_to_records_pyr(const Tin *__restrict__ src, int W, int H
         }
     }
     __syncthreads();
+    // Records are written in 16-byte chunks of consecutive labels (Lp is a
+    // multiple of 8, so a node's D part is a whole number of chunks).
+    constexpr int E = 16 / sizeof(T);
+    const int cpn = Lp / E;
     const int nn = min(32, W - x0);
     for (int r = 0; r < rows; ++r) {
         const int y = 2 * Y + r;
-        for (int idx = ty * 32 + tx; idx < nn * Lp; idx += 256) {
-            const int i = idx / Lp, l = idx - i * Lp;
-            T *d = reinterpret_cast<T *>(rec + ((size_t)y * W + x0 + i) * rec_bytes);
-            d[l] = tile[(r * Lp + l) * 33 + i];
+        for (int q = ty * 32 + tx; q < nn * cpn; q += 256) {
+            const int i = q / cpn, l0 = (q - i * cpn) * E;
+            alignas(16) T v[E];
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = tile[(r * Lp + l0 + e) * 33 + i];
+            *reinterpret_cast<uint4 *>(rec + ((size_t)y * W + x0 + i) * rec_bytes + (size_t)l0 * sizeof(T)) =
+                *reinterpret_cast<const uint4 *>(v);
         }
     }
     const int cn = min(16, cW - x0 / 2);
-    for (int idx = ty * 32 + tx; idx < cn * Lp; idx += 256) {
-        const int i = idx / Lp, l = idx - i * Lp;
-        T acc = T(0);
-        if (l < L) {
-            for (int r = 0; r < rows; ++r)
-                for (int dx = 0; dx < 2; ++dx) {
-                    if (x0 + 2 * i + dx >= W) break;
-                    acc += tile[(r * Lp + l) * 33 + 2 * i + dx];
-                }
+    for (int q = ty * 32 + tx; q < cn * cpn; q += 256) {
+        const int i = q / cpn, l0 = (q - i * cpn) * E;
+        const int dxn = min(2, W - (x0 + 2 * i));  // fine columns of this coarse node
+        alignas(16) T acc[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            acc[e] = T(0);
+            if (l0 + e < L) {
+                for (int r = 0; r < rows; ++r)
+                    for (int dx = 0; dx < dxn; ++dx) acc[e] += tile[(r * Lp + l0 + e) * 33 + 2 * i + dx];
+            }
         }
-        reinterpret_cast<T *>(crec + ((size_t)Y * cW + x0 / 2 + i) * rec_bytes)[l] = acc;
+        *reinterpret_cast<uint4 *>(crec + ((size_t)Y * cW + x0 / 2 + i) * rec_bytes + (size_t)l0 * sizeof(T)) =
+            *reinterpret_cast<const uint4 *>(acc);
+    }
+    __syncthreads();  // the tiles are refilled for the next row pair
     }
 }
 
@@ -120,25 +143,33 @@ __global__ void k_costs_to_records_pyr(const Tin *__restrict__ src, int W, int H
 template <typename T>
 __global__ void k_pyramid(const unsigned char *__restrict__ frec, int fW, int fH, unsigned char *__restrict__ crec,
                           int cW, int cH, int L, int Lp, uint32_t rec_bytes) {
-    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const size_t total = (size_t)cW * cH * Lp;
-    if (idx >= total) return;
-    const size_t node = idx / Lp;
-    const int l = (int)(idx - node * Lp);
-    const int X = (int)(node % cW), Y = (int)(node / cW);
-    T acc = T(0);
-    if (l < L) {
-        for (int dy = 0; dy < 2; ++dy) {
-            const int y = 2 * Y + dy;
-            if (y >= fH) break;
-            for (int dx = 0; dx < 2; ++dx) {
-                const int x = 2 * X + dx;
-                if (x >= fW) break;
-                acc += reinterpret_cast<const T *>(frec + ((size_t)y * fW + x) * rec_bytes)[l];
-            }
+    // One thread per (coarse node of row Y = blockIdx.y, 16-byte label chunk).
+    constexpr int E = 16 / sizeof(T);
+    const int cpn = Lp / E;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= cW * cpn) return;
+    const int X = q / cpn, l0 = (q - X * cpn) * E;
+    for (int Y = blockIdx.y; Y < cH; Y += gridDim.y) {
+    alignas(16) T acc[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) acc[e] = T(0);
+    for (int dy = 0; dy < 2; ++dy) {
+        const int y = 2 * Y + dy;
+        if (y >= fH) break;
+        for (int dx = 0; dx < 2; ++dx) {
+            const int x = 2 * X + dx;
+            if (x >= fW) break;
+            alignas(16) T v[E];
+            *reinterpret_cast<uint4 *>(v) = *reinterpret_cast<const uint4 *>(
+                frec + ((size_t)y * fW + x) * rec_bytes + (size_t)l0 * sizeof(T));
+#pragma unroll
+            for (int e = 0; e < E; ++e)
+                if (l0 + e < L) acc[e] += v[e];
         }
     }
-    reinterpret_cast<T *>(crec + node * rec_bytes)[l] = acc;
+    *reinterpret_cast<uint4 *>(crec + ((size_t)Y * cW + X) * rec_bytes + (size_t)l0 * sizeof(T)) =
+        *reinterpret_cast<const uint4 *>(acc);
+    }
 }
 
 // Materialised message initialisation of a level (used when a level runs
@@ -594,7 +625,7 @@ RecordFormat make_format(int ctype, int store, int L) {
 
 cudaError_t launch_costs_to_records(const RecordFormat &f, int cost_type, const void *src, int W, int H,
                                     unsigned char *rec, cudaStream_t s) {
-    const dim3 grid((W + 31) / 32, H), block(32, 8);
+    const dim3 grid((W + 31) / 32, (unsigned)std::min(H, 65535)), block(32, 8);
     GINF_DISPATCH_T(f, {
         const size_t smem = (size_t)f.Lp * 33 * sizeof(T);
         if (cost_type == CT_F32)
@@ -609,7 +640,7 @@ cudaError_t launch_costs_to_records(const RecordFormat &f, int cost_type, const 
 
 cudaError_t launch_costs_to_records_pyr(const RecordFormat &f, int cost_type, const void *src, int W, int H,
                                         unsigned char *rec, unsigned char *crec, int cW, cudaStream_t s) {
-    const dim3 grid((W + 31) / 32, (H + 1) / 2), block(32, 8);
+    const dim3 grid((W + 31) / 32, (unsigned)std::min((H + 1) / 2, 65535)), block(32, 8);
     GINF_DISPATCH_T(f, {
         const size_t smem = (size_t)2 * f.Lp * 33 * sizeof(T);
         if (smem > 48 * 1024) {
@@ -632,9 +663,11 @@ cudaError_t launch_costs_to_records_pyr(const RecordFormat &f, int cost_type, co
 
 cudaError_t launch_pyramid(const RecordFormat &f, const unsigned char *frec, int fW, int fH, unsigned char *crec,
                            int cW, int cH, cudaStream_t s) {
-    const size_t total = (size_t)cW * cH * f.Lp;
-    GINF_DISPATCH_T(f, { k_pyramid<T><<<blocks_for(total), kThreads, 0, s>>>(frec, fW, fH, crec, cW, cH, f.L, f.Lp,
-                                                                            f.rec_bytes); })
+    GINF_DISPATCH_T(f, {
+        const int cpn = f.Lp / (16 / (int)sizeof(T));
+        const dim3 grid(blocks_for((size_t)cW * cpn), (unsigned)std::min(cH, 65535));
+        k_pyramid<T><<<grid, kThreads, 0, s>>>(frec, fW, fH, crec, cW, cH, f.L, f.Lp, f.rec_bytes);
+    })
     return cudaGetLastError();
 }
 

@@ -331,3 +331,13 @@ def test_grids_without_or_with_tiny_interior(ginf, orc, W, H):
     assert np.array_equal(icm, orc.icm(P.D, P.V, init, 3))
     lab, e = ginf.solve(P.D, P.V, P.model, 2, 4, 2, labels=init.copy())
     assert e == pytest.approx(orc.energy(P.D, P.V, lab), rel=1e-12, abs=1e-12)
+
+
+def test_very_tall_grids(ginf, orc):
+    """More rows than a CUDA grid's y dimension holds (65535): the layout
+    transform, the fused level-1 pyramid and the sweeps walk every row."""
+    for W, H, levels in ((4, 70000, 1), (5, 140000, 3)):
+        P = synth.random_problem(W, H, 2, H)
+        want = orc.hbp(P.D, P.V, P.model, levels, 3)[0]
+        got = ginf.decode_hbp(P.D, P.V, P.model, levels, 3)
+        assert np.array_equal(got[1:-1, 1:-1], want[1:-1, 1:-1]), (W, H, levels)
