@@ -90,6 +90,8 @@ def lib():
         L.ginf_batch_run.argtypes = [_p, _p, ctypes.POINTER(Stats)]
         L.ginf_batch_config.argtypes = [_p, ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.POINTER(_i32)]
         L.ginf_batch_destroy.argtypes = [_p]
+        L.ginf_batch_enqueue.argtypes = [_p, _p]
+        L.ginf_batch_sync.argtypes = [_p]
         L.ginf_decode_bp_batch.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(_p), _i32, _i32,
                                            ctypes.POINTER(Options), ctypes.POINTER(Stats)]
         L.ginf_warmnet_create.argtypes = [ctypes.POINTER(_p), _i32, _i32, ctypes.c_uint64]
@@ -115,7 +117,8 @@ def lib():
                      "ginf_warmnet_load", "ginf_warmnet_save", "ginf_warmnet_destroy", "ginf_warmnet_num_params",
                      "ginf_warmnet_get_params", "ginf_warmnet_set_params", "ginf_warmnet_forward",
                      "ginf_warmnet_gradients", "ginf_warmnet_train_step", "ginf_hbp_level_state",
-                     "ginf_decode_hbp_learned", "ginf_decode_hbp_warm", "ginf_workspace_sync"):
+                     "ginf_decode_hbp_learned", "ginf_decode_hbp_warm", "ginf_workspace_sync",
+                     "ginf_batch_enqueue", "ginf_batch_sync"):
             getattr(L, name).restype = _i32
         _lib = L
     return _lib
@@ -318,6 +321,14 @@ class Batch:
         st = Stats()
         check(lib().ginf_batch_run(self.handle, stream, ctypes.byref(st) if want_stats else None))
         return st.as_dict() if want_stats else None
+
+    def enqueue(self, stream=None):
+        """Stream-ordered replay (returns at once; see sync())."""
+        check(lib().ginf_batch_enqueue(self.handle, stream))
+
+    def sync(self):
+        """Waits for the stream-ordered replays; raises a device error they recorded."""
+        check(lib().ginf_batch_sync(self.handle))
 
     def config(self):
         a, b, c = _i32(), _i32(), _i32()

@@ -12,6 +12,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -277,6 +278,11 @@ struct ginf_batch {
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool tuned_now = false;
+    // Stream-ordered replays: `done` follows the last one; the device status
+    // words of finished replays accumulate in `deferred`.
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+    std::atomic<int> deferred{0};
 };
 
 namespace {
@@ -576,7 +582,8 @@ ginf_status ginf_batch_create(ginf_batch **out, const ginf_grid *grids, int32_t 
     ginf_status st = GINF_OK;
     if (cudaMallocHost(&b->status_host, sizeof(int)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
+        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
         st = bfail(GINF_ERR_CUDA, "batch set-up failed");
     }
@@ -620,10 +627,61 @@ ginf_status ginf_batch_create(ginf_batch **out, const ginf_grid *grids, int32_t 
     return GINF_OK;
 }
 
+namespace {
+
+void CUDART_CB batch_replay_done(void *p) {
+    ginf_batch *b = static_cast<ginf_batch *>(p);
+    const int st = *b->status_host;
+    if (st) b->deferred.fetch_or(st);
+}
+
+ginf_status batch_status_error(int st) {
+    if (st & DEV_ERR_TIMEOUT)
+        return bfail(GINF_ERR_TIMEOUT, "a device-side wait of the batch solve exceeded its time limit");
+    return GINF_OK;
+}
+
+// Orders `s` after the batch's last stream-ordered replay and reports an
+// error one of them recorded.
+ginf_status batch_enter(ginf_batch *b, cudaStream_t s) {
+    if (b->pending) GINF_BCK(cudaStreamWaitEvent(s, b->done, 0));
+    return batch_status_error(b->deferred.exchange(0));
+}
+
+}  // namespace
+
+ginf_status ginf_batch_enqueue(ginf_batch *b, void *stream) {
+    ginf_gpu::set_last_error("");
+    if (!b || !b->exec) return bfail(GINF_ERR_INVALID_ARGUMENT, "batch is NULL or has no captured solve");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    ginf_status st = batch_enter(b, s);
+    if (st != GINF_OK) return st;
+    GINF_BCK(cudaGraphLaunch(b->exec, s));
+    GINF_BCK(cudaMemcpyAsync(b->status_host, b->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GINF_BCK(cudaLaunchHostFunc(s, batch_replay_done, b));
+    GINF_BCK(cudaEventRecord(b->done, s));
+    b->pending = true;
+    return GINF_OK;
+}
+
+ginf_status ginf_batch_sync(ginf_batch *b) {
+    ginf_gpu::set_last_error("");
+    if (!b) return bfail(GINF_ERR_INVALID_ARGUMENT, "batch is NULL");
+    if (b->pending) {
+        GINF_BCK(cudaEventSynchronize(b->done));
+        b->pending = false;
+    }
+    return batch_status_error(b->deferred.exchange(0));
+}
+
 ginf_status ginf_batch_run(ginf_batch *b, void *stream, ginf_stats *stats) {
     ginf_gpu::set_last_error("");
     if (!b || !b->exec) return bfail(GINF_ERR_INVALID_ARGUMENT, "batch is NULL or has no captured solve");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    {
+        ginf_status st = batch_enter(b, s);
+        if (st != GINF_OK) return st;
+    }
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         GINF_BCK(cudaEventRecord(b->ev0, s));
@@ -658,6 +716,8 @@ ginf_status ginf_batch_config(const ginf_batch *b, int32_t *tile_nodes, int32_t 
 
 ginf_status ginf_batch_destroy(ginf_batch *b) {
     if (!b) return GINF_OK;
+    if (b->pending) cudaEventSynchronize(b->done);
+    if (b->done) cudaEventDestroy(b->done);
     drop_graph(b);
     if (b->arena) cudaFree(b->arena);
     if (b->status_host) cudaFreeHost(b->status_host);

@@ -192,9 +192,9 @@ ginf_status ginf_stereo_costs(int32_t width, int32_t height, int32_t num_labels,
  * `iters` half-sweeps, the reference's semantics and stale-belief decode, as
  * ginf_decode_hbp with num_levels == 1).  The reference solves one grid per
  * call (src/include/bp.h:14-26); a batch solves them together in one
- * persistent cooperative launch per `sweeps_per_launch` half-sweeps, walking
- * a work list of (grid, tile) tickets, and replays the whole solve from a
- * CUDA graph captured at creation.  Grids: FP32 costs, Potts or
+ * persistent cooperative launch per label group and `sweeps_per_launch`
+ * half-sweeps, walking a work list of (grid, tile) entries, and replays the
+ * whole solve from a CUDA graph captured at creation.  Grids: FP32 costs, Potts or
  * truncated-linear smoothness, 2 <= L <= 64, all buffers device memory; the
  * plan keeps the pointers, so later runs see whatever those buffers hold.
  * The tile size and half-sweeps per launch are given in `opt` or chosen by
@@ -207,6 +207,15 @@ ginf_status ginf_batch_create(ginf_batch **batch, const ginf_grid *grids, int32_
                               int32_t iters, const ginf_options *opt);
 /* Replays the captured solve on `stream` (cudaStream_t) and waits for it. */
 ginf_status ginf_batch_run(ginf_batch *batch, void *stream, ginf_stats *stats);
+/* Stream-ordered replay: enqueues the captured solve on `stream` and returns.
+ * Labels are valid once the stream (or ginf_batch_sync) has finished; a
+ * batch's replays must not overlap one another (one stream, or a sync in
+ * between).  A device-side error is reported by ginf_batch_sync or by the
+ * next replay of the batch. */
+ginf_status ginf_batch_enqueue(ginf_batch *batch, void *stream);
+/* Waits for the batch's stream-ordered replays and reports a device-side
+ * error any of them recorded. */
+ginf_status ginf_batch_sync(ginf_batch *batch);
 /* The tile size and half-sweeps per launch in use, and whether this plan
  * measured them (1) or took them from the options or the cache (0). */
 ginf_status ginf_batch_config(const ginf_batch *batch, int32_t *tile_nodes, int32_t *sweeps_per_launch,

@@ -107,3 +107,28 @@ def test_batch_rejects_unsupported_grids(ginf):
     with pytest.raises(ginf.GinfError) as e:
         ginf.Batch([(D, V, P.model)], [lab], 4)
     assert e.value.status == ginf.ERR_UNSUPPORTED
+
+
+def test_stream_ordered_replays(ginf):
+    """Two plans replayed stream-ordered on two streams, twice each: every
+    replay equals the single-grid solves."""
+    import torch
+    iters = 7
+    probs = [_problems(70), _problems(90)]
+    want = [_single(ginf, p, iters) for p in probs]
+    labels = [[torch.zeros(D.shape[1:], dtype=torch.int32, device="cuda") for D, _, _ in p] for p in probs]
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    plans = [ginf.Batch(p, l, iters, tile_nodes=16, sweeps_per_launch=1) for p, l in zip(probs, labels)]
+    try:
+        for rep in range(2):
+            for k in range(2):
+                plans[k].enqueue(streams[k].cuda_stream)
+            for k in range(2):
+                plans[k].sync()
+                for g, (lab, w) in enumerate(zip(labels[k], want[k])):
+                    assert np.array_equal(lab.cpu().numpy(), w), (rep, k, g)
+                    lab.zero_()
+            torch.cuda.synchronize()
+    finally:
+        for pl in plans:
+            pl.close()
