@@ -1,5 +1,6 @@
 // warmnet.cu -- the learned warm start: a small convolutional network that
-// maps the costs of a coarse pyramid level to that level's BP beliefs, with
+// maps the costs of a pyramid level to the messages its nodes should start
+// from (on the beliefs' scale), with
 // hand-written tensor-core (mma.sync m16n8k16 BF16, FP32 accumulate)
 // forward, data-gradient and weight-gradient kernels, the loss, ReLU,
 // bias-gradient and Adam kernels, and a checkpoint format.
@@ -7,8 +8,9 @@
 // Network (L labels, h hidden channels): conv3x3(L->h) ReLU, conv3x3(h->h)
 // ReLU, conv3x3(h->h) ReLU, conv3x3(h->L); zero padding; activations NHWC.
 // Input x = D_t / 4^t (the level's costs per fine node), output
-// y = x + net(x), trained towards the beliefs B_t / 4^t of a long
-// hierarchical BP run.  Rounding points (mirrored by oracle/warmnet_ref.py):
+// y = x + net(x), trained towards (D_t + m) / 4^t, m the message sums of a
+// long hierarchical BP run (the finest level's, averaged per block, or the
+// level's own).  Rounding points (mirrored by oracle/warmnet_ref.py):
 // x, weights and hidden activations in BF16; sums in FP32; the output and
 // every gradient in FP32, rounded to BF16 where they feed a tensor-core
 // product.  The reference has no learned component: this whole file is new.

@@ -228,8 +228,11 @@ ginf_status ginf_decode_bp_batch(const ginf_grid *grids, int32_t *const *labels,
 /* Learned warm start for hierarchical BP (new here: the reference has no
  * learned component).  A small BF16 convolutional network (3x3 convs,
  * L -> 32 -> 32 -> 32 -> L, ReLU, FP32 accumulate, tensor-core kernels) maps
- * the costs of pyramid level t, x = D_t / 4^t, to that level's beliefs,
- * y = x + net(x) ~ B_t / 4^t.  Device buffers are FP32, [n][h][w][L]. */
+ * the costs of pyramid level t, x = D_t / 4^t, to y = x + net(x) ~
+ * (D_t + m) / 4^t, m being the sum of the messages the level's nodes should
+ * start from: the converged finest-level messages averaged per block (or
+ * the level's own beliefs; ginf_hbp_level_state produces either target).
+ * Device buffers are FP32, [n][h][w][L]. */
 typedef struct ginf_warmnet ginf_warmnet;
 ginf_status ginf_warmnet_create(ginf_warmnet **net, int32_t num_labels, int32_t hidden, uint64_t seed);
 /* Checkpoints hold the weights and the Adam state, with a checksum. */
