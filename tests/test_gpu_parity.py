@@ -341,3 +341,27 @@ def test_very_tall_grids(ginf, orc):
         want = orc.hbp(P.D, P.V, P.model, levels, 3)[0]
         got = ginf.decode_hbp(P.D, P.V, P.model, levels, 3)
         assert np.array_equal(got[1:-1, 1:-1], want[1:-1, 1:-1]), (W, H, levels)
+
+
+def test_stream_ordered_decode_and_int_grids_from_host(ginf, orc):
+    """ginf_decode_hbp stream-ordered on two workspaces / two streams with
+    pinned int32 grids read in place: equal to the oracle."""
+    import ctypes
+    import torch
+    P = synth.random_problem(90, 70, 24, 12, dtype=np.int32)
+    want, _ = orc.hbp(P.D, P.V, P.model, 3, 5)
+    D, V = torch.from_numpy(P.D).pin_memory(), torch.from_numpy(P.V).pin_memory()
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    wss = [ginf.Workspace(), ginf.Workspace()]
+    labs = [torch.zeros((70, 90), dtype=torch.int32).pin_memory() for _ in range(4)]
+    g = ginf.make_grid(D, V, P.model)
+    for i in range(4):
+        o = ginf.options(stream=streams[i % 2].cuda_stream, stream_ordered=1)
+        ginf.check(ginf.lib().ginf_decode_hbp(wss[i % 2].handle, ctypes.byref(g), 3, 5, labs[i].data_ptr(),
+                                              ctypes.byref(o), None))
+    for w in wss:
+        w.sync()
+    for i in range(4):
+        assert np.array_equal(labs[i].numpy()[1:-1, 1:-1], want[1:-1, 1:-1]), i
+    for w in wss:
+        w.close()
