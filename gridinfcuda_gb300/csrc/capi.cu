@@ -37,8 +37,6 @@ cudaError_t launch_sweep(const RecordFormat &f, const SweepConfig &cfg, SweepPar
     return cudaErrorInvalidValue;
 }
 
-bool sweep_supported(const RecordFormat &f) { return f.L >= 2 && f.L <= kMaxLabels; }
-
 }  // namespace ginf_gpu
 
 namespace {

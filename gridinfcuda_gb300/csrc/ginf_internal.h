@@ -76,7 +76,6 @@ cudaError_t launch_sweep(const RecordFormat &f, const SweepConfig &cfg, SweepPar
                          int num_sms);
 // Largest L the sweep kernels are compiled for.
 constexpr int kMaxLabels = 128;
-bool sweep_supported(const RecordFormat &f);
 
 // Auxiliary kernels (aux_kernels.cu).
 cudaError_t launch_costs_to_records(const RecordFormat &f, int cost_type, const void *src, int W, int H,
