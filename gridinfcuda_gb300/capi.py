@@ -91,6 +91,7 @@ def lib():
         L.ginf_batch_config.argtypes = [_p, ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.POINTER(_i32)]
         L.ginf_batch_destroy.argtypes = [_p]
         L.ginf_batch_enqueue.argtypes = [_p, _p]
+        L.ginf_selftest_bounded_waits.argtypes = [ctypes.POINTER(_i32), ctypes.POINTER(_i32)]
         L.ginf_batch_sync.argtypes = [_p]
         L.ginf_decode_bp_batch.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(_p), _i32, _i32,
                                            ctypes.POINTER(Options), ctypes.POINTER(Stats)]
@@ -118,7 +119,7 @@ def lib():
                      "ginf_warmnet_get_params", "ginf_warmnet_set_params", "ginf_warmnet_forward",
                      "ginf_warmnet_gradients", "ginf_warmnet_train_step", "ginf_hbp_level_state",
                      "ginf_decode_hbp_learned", "ginf_decode_hbp_warm", "ginf_workspace_sync",
-                     "ginf_batch_enqueue", "ginf_batch_sync"):
+                     "ginf_batch_enqueue", "ginf_batch_sync", "ginf_selftest_bounded_waits"):
             getattr(L, name).restype = _i32
         _lib = L
     return _lib
@@ -479,6 +480,14 @@ def decode_hbp_warm(D, V, model, levels, iters, warm_level, prediction, labels=N
                                      1 if fallback else 0, _ptr(lab)[0], ctypes.byref(o),
                                      ctypes.byref(st) if want_stats else None))
     return (lab, st.as_dict()) if want_stats else lab
+
+
+def selftest_bounded_waits():
+    """(mbarrier status, grid-barrier status) after the library's bounded
+    device waits were run into their time limit on purpose (about 2 s each)."""
+    a, b = _i32(), _i32()
+    check(lib().ginf_selftest_bounded_waits(ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value
 
 
 def version() -> str:

@@ -310,6 +310,14 @@ ginf_status ginf_decode_hbp_warm(ginf_workspace *ws, const ginf_grid *grid, int3
 #define GINF_NOALLOC_SCRATCH_BYTES (48u * 1024u * 1024u)
 ginf_status ginf_decode_bp_noalloc(const ginf_grid *grid, int32_t num_iters, int32_t *labels, void *stream);
 
+/* Diagnostic (new here): runs the library's bounded device-side waits into
+ * their time limit on purpose -- an mbarrier phase nothing completes and a
+ * grid barrier one block short -- and returns the status words they recorded
+ * (GINF_DEVICE_TIMEOUT expected in both).  Each wait gives up after about two
+ * seconds and its kernel ends normally; the device stays usable. */
+#define GINF_DEVICE_TIMEOUT 1
+ginf_status ginf_selftest_bounded_waits(int32_t *mbarrier_status, int32_t *barrier_status);
+
 #ifdef __cplusplus
 }
 #endif

@@ -365,3 +365,16 @@ def test_stream_ordered_decode_and_int_grids_from_host(ginf, orc):
         assert np.array_equal(labs[i].numpy()[1:-1, 1:-1], want[1:-1, 1:-1]), i
     for w in wss:
         w.close()
+
+
+def test_bounded_waits_time_out_and_the_device_stays_usable(ginf, orc):
+    """The mbarrier wait and the grid barrier are driven into their time
+    limit on purpose (a phase nothing completes, a barrier one block short):
+    both record the timeout status and return, and a solve afterwards is
+    still exact."""
+    mbar, barrier = ginf.selftest_bounded_waits()
+    assert mbar == 1 and barrier == 1
+    P = synth.random_problem(40, 30, 8, 21)
+    want, _ = orc.hbp(P.D, P.V, P.model, 2, 4)
+    got = ginf.decode_hbp(P.D, P.V, P.model, 2, 4)
+    assert np.array_equal(got[1:-1, 1:-1], want[1:-1, 1:-1])
