@@ -8,7 +8,11 @@
 //   out.raw: int32 W*H labels of gpuDecodeBp (30 iterations), then
 //            W*H labels of decodeHbp (3 levels x 6), then W*H labels of
 //            decodeIcmSync (2 sweeps from the BP labels), then the
-//            energy of the BP labelling as int32.
+//            energy of the BP labelling as int32; then, for the same costs
+//            as a Grid<float> with TruncLinear(1.5, 3): decodeBp (12),
+//            gpuDecodeHbp (2 levels x 5), decodeIcmAsync (2 sweeps) and
+//            gpuDecodeIcm (3 sweeps) from the decodeBp labels, W*H labels
+//            each, and the float energy of the decodeBp labelling.
 #include <cstdio>
 #include <vector>
 
@@ -45,12 +49,35 @@ int main(int argc, char **argv) {
     const int energy = grid.getLabelingCost(&bp);
     if (ginf::lastStatus() != 0) return 1;
 
+    ginf::Grid<float> fgrid(W, H, L);
+    for (int k = 0; k < L; k++)
+        for (int y = 0; y < H; y++)
+            for (int x = 0; x < W; x++)
+                fgrid.setDataCost(x, y, k, 0.25f * (float)costs[(size_t)x + (size_t)W * y + (size_t)W * H * k]);
+    fgrid.useSmoothnessTruncLinear(1.5f, 3.0f);
+    ginf::Matrix<int> fbp(2, W, H), fhbp(2, W, H), ficma(2, W, H), ficmg(2, W, H);
+    ginf::decodeBp(&fgrid, 12, &fbp);
+    if (ginf::lastStatus() != 0) return 1;
+    ginf::gpuDecodeHbp(&fgrid, 2, 5, &fhbp);
+    if (ginf::lastStatus() != 0) return 1;
+    ginf::decodeIcmAsync(&fgrid, &fbp, 2, &ficma);
+    if (ginf::lastStatus() != 0) return 1;
+    ginf::gpuDecodeIcm(&fgrid, &fbp, 3, &ficmg);
+    if (ginf::lastStatus() != 0) return 1;
+    const float fenergy = fgrid.getLabelingCost(&fbp);
+    if (ginf::lastStatus() != 0) return 1;
+
     FILE *o = std::fopen(argv[2], "wb");
     if (!o) return 2;
     std::fwrite(bp.data, sizeof(int), (size_t)W * H, o);
     std::fwrite(hbp.data, sizeof(int), (size_t)W * H, o);
     std::fwrite(icm.data, sizeof(int), (size_t)W * H, o);
     std::fwrite(&energy, sizeof(int), 1, o);
+    std::fwrite(fbp.data, sizeof(int), (size_t)W * H, o);
+    std::fwrite(fhbp.data, sizeof(int), (size_t)W * H, o);
+    std::fwrite(ficma.data, sizeof(int), (size_t)W * H, o);
+    std::fwrite(ficmg.data, sizeof(int), (size_t)W * H, o);
+    std::fwrite(&fenergy, sizeof(float), 1, o);
     std::fclose(o);
     return 0;
 }

@@ -31,7 +31,11 @@ def test_cpp_program_matches_oracle(ginf, orc, built_lib, tmp_path):
     assert r.returncode == 0, r.stderr
     res = np.fromfile(out, np.int32)
     n = W * H
-    bp, hbp, icm, energy = res[:n].reshape(H, W), res[n:2 * n].reshape(H, W), res[2 * n:3 * n].reshape(H, W), res[-1]
+    bp, hbp, icm, energy = res[:n].reshape(H, W), res[n:2 * n].reshape(H, W), res[2 * n:3 * n].reshape(H, W), \
+        res[3 * n]
+    f = res[3 * n + 1:]
+    fbp, fhbp, ficma, ficmg = (f[i * n:(i + 1) * n].reshape(H, W) for i in range(4))
+    fenergy = f[4 * n:4 * n + 1].view(np.float32)[0]
     V = synth.sm_table(L, synth.TRUNC_LINEAR, 10, 20, dtype=np.int32)
     want_bp, _ = orc.hbp(D, V, synth.TRUNC_LINEAR, 1, 30)
     want_hbp, _ = orc.hbp(D, V, synth.TRUNC_LINEAR, 3, 6)
@@ -39,3 +43,12 @@ def test_cpp_program_matches_oracle(ginf, orc, built_lib, tmp_path):
     assert np.array_equal(hbp, want_hbp)
     assert np.array_equal(icm, orc.icm(D, V, want_bp, 2))
     assert energy == orc.energy(D, V, want_bp, exact_type=True)
+    # The same costs as a Grid<float>: decodeBp, gpuDecodeHbp, decodeIcmAsync, gpuDecodeIcm.
+    Df = (np.float32(0.25) * D.astype(np.float32)).astype(np.float32)
+    Vf = synth.sm_table(L, synth.TRUNC_LINEAR, 1.5, 3.0)
+    want_fbp, _ = orc.hbp(Df, Vf, synth.TRUNC_LINEAR, 1, 12)
+    assert np.array_equal(fbp, want_fbp)
+    assert np.array_equal(fhbp, orc.hbp(Df, Vf, synth.TRUNC_LINEAR, 2, 5)[0])
+    assert np.array_equal(ficma, orc.icm(Df, Vf, want_fbp, 2, asynchronous=True))
+    assert np.array_equal(ficmg, orc.icm(Df, Vf, want_fbp, 3))
+    assert fenergy == pytest.approx(orc.energy(Df, Vf, want_fbp), rel=1e-6)
