@@ -365,7 +365,10 @@ __global__ void __launch_bounds__(kThreads, 6)
         const size_t i = (size_t)y * W + x;
         const bool need = !chg_in || (chg_in[i - W] | chg_in[i + W] | chg_in[i - 1] | chg_in[i + 1]) != 0;
         const T *D = reinterpret_cast<const T *>(rec + i * rec_bytes);
-        int bl = icm_node<T, LANES>(D, W, L, Lp, Vs, old_lab, x, y, g, status, need);
+        // A warp none of whose nodes needs the minimisation skips it whole
+        // (the test is warp-uniform, so the lane combine stays convergent).
+        int bl = 0;
+        if (__any_sync(0xffffffffu, need)) bl = icm_node<T, LANES>(D, W, L, Lp, Vs, old_lab, x, y, g, status, need);
         if (act && g == 0) {
             const int prev = old_lab[i];
             if (!need) bl = prev;
