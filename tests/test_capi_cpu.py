@@ -86,3 +86,39 @@ def test_default_options_layout(built_lib):
     assert ctypes.sizeof(capi.Grid) == 6 * 4 + 2 * 8
     assert ctypes.sizeof(capi.Stats) == 8 * 8 + 7 * 8
     assert capi.version().startswith("gridinfcuda-gb300")
+
+
+def test_option_and_entry_point_validation_without_device(built_lib):
+    """Bad options and arguments of the newer entry points are rejected with
+    GINF_ERR_INVALID_ARGUMENT / GINF_ERR_UNSUPPORTED before any device work."""
+    import numpy as np
+    from gridinfcuda_gb300 import capi
+    L = capi.lib()
+    D = np.zeros((8, 6, 5), np.float32)
+    V = np.zeros(64, np.float32)
+    lab = np.zeros((6, 5), np.int32)
+    g = capi.Grid(5, 6, 8, capi.F32, capi.TRUNC_LINEAR, capi.HOST, D.ctypes.data, V.ctypes.data)
+
+    def hbp(**opt):
+        o = capi.options(**opt)
+        return L.ginf_decode_hbp(None, ctypes.byref(g), 2, 3, lab.ctypes.data, ctypes.byref(o), None)
+
+    assert hbp(tile_nodes=12) == capi.ERR_INVALID_ARGUMENT
+    assert hbp(host_access=5) == capi.ERR_INVALID_ARGUMENT and b"host_access" in L.ginf_last_error()
+    assert hbp(stream_ordered=1) == capi.ERR_INVALID_ARGUMENT and b"workspace" in L.ginf_last_error()
+    assert hbp(store=capi.STORE_F16, compute_type=capi.F64) == capi.ERR_UNSUPPORTED
+    # seeded hierarchical BP: the prediction buffer and the level range
+    o = capi.options()
+    assert L.ginf_decode_hbp_warm(None, ctypes.byref(g), 3, 2, 1, 0, 0, None, 1, lab.ctypes.data,
+                                  ctypes.byref(o), None) == capi.ERR_INVALID_ARGUMENT
+    assert L.ginf_decode_hbp_learned(None, ctypes.byref(g), 3, 2, 1, 0, -1, None, lab.ctypes.data,
+                                     ctypes.byref(o), None) == capi.ERR_INVALID_ARGUMENT
+    # batches: only device buffers, 2 <= L <= 64
+    grids = (capi.Grid * 1)(g)
+    labs = (ctypes.c_void_p * 1)(lab.ctypes.data)
+    h = ctypes.c_void_p()
+    assert L.ginf_batch_create(ctypes.byref(h), grids, labs, 1, 5, None) == capi.ERR_INVALID_ARGUMENT
+    assert L.ginf_batch_sync(None) == capi.ERR_INVALID_ARGUMENT
+    assert L.ginf_workspace_sync(None) == capi.ERR_INVALID_ARGUMENT
+    # the bounded-wait self-test needs its output pointers
+    assert L.ginf_selftest_bounded_waits(None, None) == capi.ERR_INVALID_ARGUMENT
