@@ -92,7 +92,7 @@ __device__ __forceinline__ SweepParams batch_params(const BatchLaunch &b, const 
 // binary search over the tile bases, kept in shared memory).  Between
 // half-sweeps each block waits for its own bulk stores, fences them against
 // the next half-sweep's bulk loads and meets the others at the grid barrier.
-template <int NW, int LM, bool EXACT>
+template <int NW, int LM, bool EXACT, bool DIRECT = false>
 __global__ void __launch_bounds__(NW * 32) batch_kernel(const BatchLaunch b) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t full_bar;
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(NW * 32) batch_kernel(const BatchLaunch b) {
             tile_load<NW>(p, t - base, smem, &full_bar);
         }
         for (; t < b.total_tiles; t += gridDim.x) {
-            if (!tile_finish<float, float, LM, EXACT, NW, KIND_LINEAR>(
+            if (!tile_finish<float, float, LM, EXACT, NW, KIND_LINEAR, DIRECT>(
                     p, table_consts<float, KIND_LINEAR>(p.V, EXACT ? LM : p.L), t - base, smem, &full_bar, parity))
                 return;
             const int tn = t + gridDim.x;
@@ -342,9 +342,9 @@ std::vector<BatchItem> make_items(ginf_batch *b, int tile_nodes) {
     return items;
 }
 
-template <int NW, int LM, bool EXACT>
+template <int NW, int LM, bool EXACT, bool DIRECT = false>
 cudaError_t launch_batch(BatchLaunch bl, uint32_t max_slot, int num_sms, cudaStream_t s) {
-    auto kern = batch_kernel<NW, LM, EXACT>;
+    auto kern = batch_kernel<NW, LM, EXACT, DIRECT>;
     bl.tile_smem = (uint32_t)(((size_t)NW * 8 * max_slot + 15) / 16 * 16);
     const size_t bases_bytes = sizeof(int) * (size_t)bl.count;
     bl.bases_in_smem = bases_bytes <= 16 * 1024 ? 1 : 0;
@@ -372,6 +372,11 @@ cudaError_t launch_batch(BatchLaunch bl, uint32_t max_slot, int num_sms, cudaStr
 
 template <int LM, bool EXACT>
 cudaError_t launch_batch_nw(int tile_nodes, const BatchLaunch &bl, uint32_t max_slot, int num_sms, cudaStream_t s) {
+    if constexpr (LM == 16 && EXACT) {
+        // 64-byte messages: ordinary stores on large groups (see tile_finish).
+        if (tile_nodes == 16 && bl.total_tiles >= kDirectStoreTiles)
+            return launch_batch<2, LM, EXACT, true>(bl, max_slot, num_sms, s);
+    }
     if (tile_nodes == 8) return launch_batch<1, LM, EXACT>(bl, max_slot, num_sms, s);
     if (tile_nodes == 32) return launch_batch<4, LM, EXACT>(bl, max_slot, num_sms, s);
     return launch_batch<2, LM, EXACT>(bl, max_slot, num_sms, s);

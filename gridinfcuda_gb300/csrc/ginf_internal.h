@@ -74,6 +74,10 @@ struct SweepConfig {
 // Launch one half-sweep; returns the kernel launch error.
 cudaError_t launch_sweep(const RecordFormat &f, const SweepConfig &cfg, SweepParams p, cudaStream_t s,
                          int num_sms);
+// Launches of 64-byte-message kernels (L = 16, FP32) with at least this many
+// 16-node tiles store their messages with ordinary stores (see tile_finish).
+constexpr long kDirectStoreTiles = 16384;
+
 // Largest L the sweep kernels are compiled for.
 constexpr int kMaxLabels = 128;
 

@@ -630,7 +630,11 @@ __device__ __forceinline__ void tile_load(const SweepParams &p, int t, unsigned 
 // the truncated-linear update only (the hot path, with a clean register
 // allocation), the standard truncated-quadratic update (window radius 8, or
 // 4 for KIND_QUAD4), or every rule.
-template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND>
+// DIRECT (64-byte messages only): the messages leave through ordinary
+// 16-byte stores instead of one bulk copy each, which pays on large launches
+// (the copy engine's per-copy cost dominates 64-byte copies) and not on small,
+// L2-resident ones.
+template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND, bool DIRECT = false>
 __device__ __forceinline__ bool tile_finish(const SweepParams &p, const TableConsts<T> &tc, int t,
                                             unsigned char *smem, uint64_t *bar, uint32_t &parity) {
     const int dir = (threadIdx.x & 31) >> 3;
@@ -667,17 +671,34 @@ __device__ __forceinline__ bool tile_finish(const SweepParams &p, const TableCon
             else message_std_quad<T, M, LMAX>(p, slot, L, dir, tc.scale, tc.trunc);
         }
     }
-    // Every lane orders its shared-memory writes before the async-proxy
-    // reads of the bulk stores (lanes may store slots other lanes wrote).
-    fence_proxy_async_shared();
-    __syncwarp();
-    if (act) {
-        if (dir == 0 && p.write_labels) p.labels[(size_t)y * p.W + x] = label;
-        const int qx = x + dir_dx(dir), qy = y + dir_dy(dir);
-        unsigned char *dst = p.rec + ((size_t)qy * p.W + qx) * p.rec_bytes + p.d_bytes + opp_dir(dir) * p.m_bytes;
-        bulk_store(dst, slot + p.d_bytes + dir * p.m_bytes, p.m_bytes);
-        bulk_commit();
-        bulk_wait_read_all();
+    if constexpr (DIRECT) {
+        static_assert(EXACT && LMAX * sizeof(M) == 64, "direct stores are for 64-byte messages");
+        __syncwarp();
+        if (act) {
+            if (dir == 0 && p.write_labels) p.labels[(size_t)y * p.W + x] = label;
+            const int qx = x + dir_dx(dir), qy = y + dir_dy(dir);
+            uint4 *dst = reinterpret_cast<uint4 *>(p.rec + ((size_t)qy * p.W + qx) * p.rec_bytes + p.d_bytes +
+                                                   opp_dir(dir) * p.m_bytes);
+            const uint4 *src = reinterpret_cast<const uint4 *>(slot + p.d_bytes + dir * p.m_bytes);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) dst[c] = src[c];
+        }
+        // The slots just read are refilled by the next tile's bulk copies.
+        fence_proxy_async_shared();
+    } else {
+        // Every lane orders its shared-memory writes before the async-proxy
+        // reads of the bulk stores (lanes may store slots other lanes wrote).
+        fence_proxy_async_shared();
+        __syncwarp();
+        if (act) {
+            if (dir == 0 && p.write_labels) p.labels[(size_t)y * p.W + x] = label;
+            const int qx = x + dir_dx(dir), qy = y + dir_dy(dir);
+            unsigned char *dst =
+                p.rec + ((size_t)qy * p.W + qx) * p.rec_bytes + p.d_bytes + opp_dir(dir) * p.m_bytes;
+            bulk_store(dst, slot + p.d_bytes + dir * p.m_bytes, p.m_bytes);
+            bulk_commit();
+            bulk_wait_read_all();
+        }
     }
     __syncthreads();
     return true;
@@ -685,7 +706,7 @@ __device__ __forceinline__ bool tile_finish(const SweepParams &p, const TableCon
 
 // One checkerboard half-sweep of one level: blocks take tiles in turn, each
 // issuing the copies of its next tile as soon as the current one is done.
-template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND>
+template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND, bool DIRECT = false>
 __global__ void __launch_bounds__(NW * 32) sweep_kernel(const SweepParams p) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t full_bar;
@@ -704,16 +725,16 @@ __global__ void __launch_bounds__(NW * 32) sweep_kernel(const SweepParams p) {
     if (t < p.num_tiles) tile_load<NW>(p, t, smem, &full_bar);
     uint32_t parity = 0;
     for (; t < p.num_tiles; t += gridDim.x) {
-        if (!tile_finish<T, M, LMAX, EXACT, NW, KIND>(p, tc, t, smem, &full_bar, parity)) return;
+        if (!tile_finish<T, M, LMAX, EXACT, NW, KIND, DIRECT>(p, tc, t, smem, &full_bar, parity)) return;
         const int tn = t + gridDim.x;
         if (tn < p.num_tiles) tile_load<NW>(p, tn, smem, &full_bar);
     }
     bulk_wait_all();
 }
 
-template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND>
+template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND, bool DIRECT = false>
 cudaError_t launch_one(const SweepParams &params, uint32_t slot_bytes, cudaStream_t s, int num_sms) {
-    auto kern = sweep_kernel<T, M, LMAX, EXACT, NW, KIND>;
+    auto kern = sweep_kernel<T, M, LMAX, EXACT, NW, KIND, DIRECT>;
     // The tiling follows the variant actually launched (8*NW nodes per tile).
     SweepParams p = params;
     const int n1 = p.W >= 3 ? (p.W - 3) / 2 + 1 : 0;
@@ -775,6 +796,12 @@ cudaError_t launch_variant(const RecordFormat &f, const SweepConfig &cfg, const 
     if constexpr (std::is_same<T, float>::value) {
         if (cfg.nt == 8) return launch_one<T, M, LM, true, 1, KIND_LINEAR>(p, f.slot_bytes, s, num_sms);
         if (cfg.nt == 32) return launch_one<T, M, LM, true, 4, KIND_LINEAR>(p, f.slot_bytes, s, num_sms);
+        if constexpr (LM * sizeof(M) == 64) {
+            const int n1 = p.W >= 3 ? (p.W - 3) / 2 + 1 : 0;
+            const long tiles = p.H >= 3 ? (long)(p.H - 2) * ((n1 + 15) / 16) : 0;
+            if (tiles >= kDirectStoreTiles)
+                return launch_one<T, M, LM, true, 2, KIND_LINEAR, true>(p, f.slot_bytes, s, num_sms);
+        }
     }
     return launch_one<T, M, LM, true, 2, KIND_LINEAR>(p, f.slot_bytes, s, num_sms);
 }
