@@ -565,11 +565,13 @@ __device__ __forceinline__ TableConsts<T> table_consts(const void *V, int L) {
 // allocation), the standard truncated-quadratic update (window radius 8, or
 // 4 for KIND_QUAD4), or every rule.  Returns false, block-uniformly, when the
 // bounded wait for the tile's copies gave up.
-template <int NW>
+// SPL warps share each group of eight nodes (1, or 2 for the split kernel:
+// warp w serves nodes (w / SPL) * 8 + k).
+template <int NW, int SPL = 1>
 __device__ __forceinline__ bool tile_node(const SweepParams &p, int t, int &x, int &y) {
-    const int node = (threadIdx.x >> 5) * 8 + (threadIdx.x & 7);
+    const int node = ((threadIdx.x >> 5) / SPL) * 8 + (threadIdx.x & 7);
     y = 1 + t / p.tiles_per_row;
-    x = ((y + p.iter) & 1) + 1 + 2 * ((t % p.tiles_per_row) * NW * 8 + node);
+    x = ((y + p.iter) & 1) + 1 + 2 * ((t % p.tiles_per_row) * (NW / SPL) * 8 + node);
     return x <= p.W - 2;
 }
 
@@ -578,13 +580,15 @@ __device__ __forceinline__ bool tile_node(const SweepParams &p, int t, int &x, i
 // node's padded shared-memory slot with one bulk TMA copy (the first sweep of
 // a level fetches D and, per lane, one incoming slot from the coarser level
 // instead).
-template <int NW>
+template <int NW, int SPL = 1>
 __device__ __forceinline__ void tile_load(const SweepParams &p, int t, unsigned char *smem, uint64_t *bar) {
     const int dir = (threadIdx.x & 31) >> 3;
-    const int node = (threadIdx.x >> 5) * 8 + (threadIdx.x & 7);
+    const int node = ((threadIdx.x >> 5) / SPL) * 8 + (threadIdx.x & 7);
     unsigned char *slot = smem + (size_t)node * p.slot_bytes;
     int x, y;
-    const bool act = tile_node<NW>(p, t, x, y);
+    // With SPL warps per node group only the first of them issues copies;
+    // every thread still arrives on the mbarrier.
+    const bool act = tile_node<NW, SPL>(p, t, x, y) && ((threadIdx.x >> 5) % SPL) == 0;
     uint32_t bytes = 0;
     bool want = false;
     if (act) {
@@ -704,6 +708,211 @@ __device__ __forceinline__ bool tile_finish(const SweepParams &p, const TableCon
     return true;
 }
 
+// ---------------------------------------------------------------------------
+// Split kernel: FP32 records, L = 128, truncated quadratic with the windowed
+// transform (window radius QW).  A lane holding a whole 128-label message
+// needs ~235 registers, which leaves 8 warps per SM and the kernel
+// latency-bound; here two warps serve each group of eight nodes and a lane
+// (k, dir) of warp 2g + hf computes labels [64 hf, 64 hf + 64) of node
+// g * 8 + k's message towards dir, with h read over that range plus a QW-label
+// halo.  Results are bit-identical to message_quad_window:
+//   - min(h) is the fminf of the two halves' minima (fminf is exact);
+//   - each output value is the same expression over the same h values (h is
+//     +inf outside [0, L), as the single-lane form's missing taps);
+//   - the mean's sum stays sequential in label order: half 0 sums its 64
+//     outputs from zero, half 1 continues from that partial sum;
+//   - the argmin combines the halves' first minima by (value, label).
+// Shared words exchanged between the two warps of a group.
+template <int NW>
+struct SplitXch {
+    float minh[NW][32];      // lane's minimum of h over its own half
+    float sum[NW / 2][32];   // half 0's sequential partial sum of its outputs
+    float mean[NW / 2][32];  // the finished mean, from half 1
+    float best[NW][8];       // node's belief minimum over the warp's half
+    int label[NW][8];        // and its first label
+};
+
+// Belief over labels [base, base + 64) of one node by its four lanes of one
+// warp (chunks base + 4 (4 j + dir)); see belief_part.
+__device__ __forceinline__ void belief_half(const SweepParams &p, unsigned char *slot, int dir, int base, float &best,
+                                            int &bl) {
+    const unsigned char *mb = slot + p.d_bytes;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int c = base + (4 * j + dir) * 4;
+        float v[4], a[4];
+        load_t<float, 4>(slot + c * sizeof(float), v);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            MIO<float, float>::load(mb + e * p.m_bytes + c * sizeof(float), a);
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) v[kk] = v[kk] + a[kk];
+        }
+        store_t<float, 4>(slot + c * sizeof(float), v);
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+            if (bl == 0x7fffffff || v[kk] < best) {
+                best = v[kk];
+                bl = c + kk;
+            }
+        }
+    }
+}
+
+// One tile of the split kernel (8 * NW / 2 nodes).  Block barriers: after the
+// beliefs (the halo of h reads the other half's), after h is loaded (the
+// outgoing messages overwrite the incoming slots), after half 0's partial
+// sum, and after half 1's mean.  Each half bulk-stores its own 256 bytes.
+template <int NW, int QW>
+__device__ __forceinline__ bool tile_finish_split(const SweepParams &p, const TableConsts<float> &tc, int t,
+                                                  unsigned char *smem, uint64_t *bar, uint32_t &parity,
+                                                  SplitXch<NW> &xs) {
+    constexpr int L = 128, HL = 64, NH = HL + 2 * QW;
+    static_assert(QW % 4 == 0, "the halo is whole 16-byte chunks");
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int hf = w & 1, g = w >> 1;
+    const int dir = lane >> 3, k = lane & 7;
+    const int base = hf * HL;
+    unsigned char *slot = smem + (size_t)(g * 8 + k) * p.slot_bytes;
+    unsigned char *md = slot + p.d_bytes + dir * p.m_bytes;
+    const bool got = mbar_wait_bounded(bar, parity, p.status);
+    parity ^= 1u;
+    if (!__syncthreads_and(got)) return false;
+    int x, y;
+    const bool act = tile_node<NW, 2>(p, t, x, y);
+    // Each half zeroes, then sums, only its own labels of the incoming slots.
+    if (act && ((zero_mask(p, x, y) >> dir) & 1u)) zero_bytes(md + base * sizeof(float), HL * sizeof(float));
+    __syncwarp();
+    float best = pos_inf<float>();
+    int label = 0x7fffffff;
+    if (act) belief_half(p, slot, dir, base, best, label);
+    argmin_combine(best, label);
+    if (dir == 0) {
+        xs.best[w][k] = best;
+        xs.label[w][k] = label;
+    }
+    __syncthreads();
+    {
+        const float ob = xs.best[w ^ 1][k];
+        const int ol = xs.label[w ^ 1][k];
+        if (ol != 0x7fffffff && (label == 0x7fffffff || ob < best || (!(best < ob) && ol < label))) label = ol;
+    }
+    float h[NH];
+    float mloc = pos_inf<float>();
+    if (act) {
+#pragma unroll
+        for (int c = 0; c < NH; c += 4) {
+            // Chunk labels base - QW + c .. +3: below 0 only for half 0's
+            // leading halo, at or above L only for half 1's trailing halo.
+            const bool in = (c >= QW || hf == 1) && (c < HL + QW || hf == 0);
+            if (in) {
+                const int j0 = base - QW + c;
+                float a[4], f[4];
+                MIO<float, float>::load(md + j0 * sizeof(float), a);
+                load_t<float, 4>(slot + j0 * sizeof(float), f);
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) h[c + kk] = f[kk] - a[kk];
+            } else {
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) h[c + kk] = pos_inf<float>();
+            }
+        }
+#pragma unroll
+        for (int i = QW; i < QW + HL; ++i) mloc = fminf(mloc, h[i]);
+    }
+    xs.minh[w][lane] = mloc;
+    __syncthreads();
+    // Outputs go straight into the lane's half of the incoming slot: final
+    // with the minimum subtracted, unnormalised (and corrected below) with
+    // the mean subtracted.
+    const bool norm_min = p.norm_min != 0;
+    unsigned char *mh = md + base * sizeof(float);
+    if (act) {
+        const float minh = hf == 0 ? fminf(mloc, xs.minh[w ^ 1][lane]) : fminf(xs.minh[w ^ 1][lane], mloc);
+        const float cap = minh + tc.trunc;
+        const float shift = norm_min ? minh + tc.vtap[0] : 0.f;
+        float sum = 0.f;
+#pragma unroll
+        for (int c = 0; c < HL; c += 4) {
+            float r[4];
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+                const int ii = c + kk + QW;
+                float m = fminf(cap, h[ii] + tc.vtap[0]);
+#pragma unroll
+                for (int k2 = 1; k2 <= QW; ++k2) m = fminf(m, fminf(h[ii - k2], h[ii + k2]) + tc.vtap[k2]);
+                sum += m;
+                r[kk] = m - shift;
+            }
+            MIO<float, float>::store(mh + c * sizeof(float), r);
+        }
+        if (hf == 0) xs.sum[g][lane] = sum;
+    }
+    if (!norm_min) {
+        __syncthreads();
+        if (act && hf == 1) {
+            float s = xs.sum[g][lane];
+#pragma unroll
+            for (int c = 0; c < HL; c += 4) {
+                float r[4];
+                MIO<float, float>::load(mh + c * sizeof(float), r);
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) s += r[kk];
+            }
+            xs.mean[g][lane] = mean_of<float, L, true>(s, L);
+        }
+        __syncthreads();
+        if (act) {
+            const float val = xs.mean[g][lane];
+#pragma unroll
+            for (int c = 0; c < HL; c += 4) {
+                float r[4];
+                MIO<float, float>::load(mh + c * sizeof(float), r);
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) r[kk] -= val;
+                MIO<float, float>::store(mh + c * sizeof(float), r);
+            }
+        }
+    }
+    // Each lane stores only what it wrote itself.
+    fence_proxy_async_shared();
+    if (act) {
+        if (hf == 0 && dir == 0 && p.write_labels) p.labels[(size_t)y * p.W + x] = label;
+        const int qx = x + dir_dx(dir), qy = y + dir_dy(dir);
+        unsigned char *dst = p.rec + ((size_t)qy * p.W + qx) * p.rec_bytes + p.d_bytes + opp_dir(dir) * p.m_bytes;
+        bulk_store(dst + base * sizeof(float), mh, HL * sizeof(float));
+        bulk_commit();
+        bulk_wait_read_all();
+    }
+    __syncthreads();
+    return true;
+}
+
+template <int NW, int QW>
+__global__ void __launch_bounds__(NW * 32, 5) sweep_kernel_split(const SweepParams p) {
+    static_assert(NW % 2 == 0, "warps come in pairs");
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t full_bar;
+    __shared__ SplitXch<NW> xs;
+    launch_dependents();
+    const TableConsts<float> tc = table_consts<float, KIND_QUAD>(p.V, 128);
+    if (threadIdx.x == 0) {
+        mbar_init(&full_bar, NW * 32);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    grid_dependency_wait();
+    int t = blockIdx.x;
+    if (t < p.num_tiles) tile_load<NW, 2>(p, t, smem, &full_bar);
+    uint32_t parity = 0;
+    for (; t < p.num_tiles; t += gridDim.x) {
+        if (!tile_finish_split<NW, QW>(p, tc, t, smem, &full_bar, parity, xs)) return;
+        const int tn = t + gridDim.x;
+        if (tn < p.num_tiles) tile_load<NW, 2>(p, tn, smem, &full_bar);
+    }
+    bulk_wait_all();
+}
+
 // One checkerboard half-sweep of one level: blocks take tiles in turn, each
 // issuing the copies of its next tile as soon as the current one is done.
 template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND, bool DIRECT = false>
@@ -732,18 +941,28 @@ __global__ void __launch_bounds__(NW * 32) sweep_kernel(const SweepParams p) {
     bulk_wait_all();
 }
 
-template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND, bool DIRECT = false>
-cudaError_t launch_one(const SweepParams &params, uint32_t slot_bytes, cudaStream_t s, int num_sms) {
-    auto kern = sweep_kernel<T, M, LMAX, EXACT, NW, KIND, DIRECT>;
-    // The tiling follows the variant actually launched (8*NW nodes per tile).
+// Per-kernel launch state: the largest dynamic shared-memory size set so far
+// and the occupancy last computed.
+struct LaunchCache {
+    size_t configured = 0;
+    int occ_smem = -1, occ = 0;
+};
+
+// Launches one half-sweep kernel over tiles of `nodes` nodes, NW warps per
+// block, one block per resident slot of every SM (fewer if there are fewer
+// tiles).
+template <typename K>
+cudaError_t launch_tiles(K kern, LaunchCache &lc_state, int NW, int nodes, const SweepParams &params,
+                         uint32_t slot_bytes, cudaStream_t s, int num_sms) {
+    // The tiling follows the variant actually launched.
     SweepParams p = params;
     const int n1 = p.W >= 3 ? (p.W - 3) / 2 + 1 : 0;
-    p.tiles_per_row = (n1 + NW * 8 - 1) / (NW * 8);
+    p.tiles_per_row = (n1 + nodes - 1) / nodes;
     p.num_tiles = p.H >= 3 ? (p.H - 2) * p.tiles_per_row : 0;
     if (p.num_tiles <= 0) return cudaSuccess;
-    const size_t smem = (size_t)NW * 8 * slot_bytes;
-    static size_t configured = 0;  // largest dynamic smem size set so far for this instantiation
-    static int occ_cache_smem = -1, occ_cache = 0;
+    const size_t smem = (size_t)nodes * slot_bytes;
+    size_t &configured = lc_state.configured;
+    int &occ_cache_smem = lc_state.occ_smem, &occ_cache = lc_state.occ;
     if (smem > configured) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
@@ -777,6 +996,19 @@ cudaError_t launch_one(const SweepParams &params, uint32_t slot_bytes, cudaStrea
     return cudaLaunchKernelEx(&lc, kern, p);
 }
 
+template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND, bool DIRECT = false>
+cudaError_t launch_one(const SweepParams &params, uint32_t slot_bytes, cudaStream_t s, int num_sms) {
+    static LaunchCache cache;
+    return launch_tiles(sweep_kernel<T, M, LMAX, EXACT, NW, KIND, DIRECT>, cache, NW, NW * 8, params, slot_bytes, s,
+                        num_sms);
+}
+
+template <int NW, int QW>
+cudaError_t launch_split(const SweepParams &params, uint32_t slot_bytes, cudaStream_t s, int num_sms) {
+    static LaunchCache cache;
+    return launch_tiles(sweep_kernel_split<NW, QW>, cache, NW, NW / 2 * 8, params, slot_bytes, s, num_sms);
+}
+
 template <typename T, typename M, int LM>
 cudaError_t launch_variant(const RecordFormat &f, const SweepConfig &cfg, const SweepParams &p, cudaStream_t s,
                            int num_sms) {
@@ -784,6 +1016,11 @@ cudaError_t launch_variant(const RecordFormat &f, const SweepConfig &cfg, const 
     if (p.mode == MODE_STD_QUAD) {
         // The host measured the truncation radius (quad_radius_host); radius-4
         // windows run the cheaper 9-tap kernel.
+        if constexpr (std::is_same<T, float>::value && std::is_same<M, float>::value && LM == 128) {
+            // FP32 records at L = 128: two warps per eight nodes (register relief).
+            if (exact && p.quad_radius <= kQuadWindowSmall) return launch_split<4, 4>(p, f.slot_bytes, s, num_sms);
+            if (exact && p.quad_radius <= kQuadWindow) return launch_split<4, 8>(p, f.slot_bytes, s, num_sms);
+        }
         if (p.quad_radius <= kQuadWindowSmall) {
             if (exact) return launch_one<T, M, LM, true, 2, KIND_QUAD4>(p, f.slot_bytes, s, num_sms);
             return launch_one<T, M, LM, false, 2, KIND_QUAD4>(p, f.slot_bytes, s, num_sms);
