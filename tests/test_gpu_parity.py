@@ -241,19 +241,22 @@ def test_windowed_quadratic_equals_min_convolution(ginf):
     whole table: bit-identical to the O(L^2) min-convolution of the same table.
     FP32 records at L = 128 run the split kernel (two warps per eight nodes):
     radius 4 (trunc 25) and radius 7 (trunc 50) windows, the mean and the
-    minimum subtracted, 37- and 70-wide grids (partial last tiles), two levels
-    (the coarse-to-fine first sweep)."""
-    cases = [(128, 25.0, 37, 23, ginf.NORM_MEAN), (128, 25.0, 37, 23, ginf.NORM_MIN),
-             (128, 50.0, 70, 41, ginf.NORM_MEAN), (128, 50.0, 70, 41, ginf.NORM_MIN),
-             (17, 9.0, 37, 23, ginf.NORM_MEAN), (64, 2.0, 37, 23, ginf.NORM_MEAN)]
-    for L, trunc, W, H, norm in cases:
+    minimum subtracted, FP32 and FP16 messages, 37- and 70-wide grids
+    (partial last tiles), two levels (the coarse-to-fine first sweep)."""
+    F32, F16 = ginf.STORE_NATIVE, ginf.STORE_F16
+    cases = [(128, 25.0, 37, 23, ginf.NORM_MEAN, F32), (128, 25.0, 37, 23, ginf.NORM_MIN, F32),
+             (128, 50.0, 70, 41, ginf.NORM_MEAN, F32), (128, 50.0, 70, 41, ginf.NORM_MIN, F32),
+             (128, 25.0, 37, 23, ginf.NORM_MIN, F16), (128, 50.0, 70, 41, ginf.NORM_MIN, F16),
+             (17, 9.0, 37, 23, ginf.NORM_MEAN, F32), (64, 2.0, 37, 23, ginf.NORM_MEAN, F32),
+             (64, 25.0, 37, 23, ginf.NORM_MIN, F16)]
+    for L, trunc, W, H, norm, store in cases:
         P = synth.random_problem(W, H, L, 40 + L, model=synth.TRUNC_QUAD, scale=1.0, trunc=trunc, cost_max=30.0)
-        lq, mq = ginf.decode_hbp(P.D, P.V, synth.TRUNC_QUAD, 2, 5, want_msgs=True, rule=ginf.RULE_STANDARD,
-                                 normalize=norm)
-        lb, mb = ginf.decode_hbp(P.D, P.V, synth.EXPLICIT, 2, 5, want_msgs=True, rule=ginf.RULE_STANDARD,
-                                 normalize=norm)
-        assert np.array_equal(lq, lb), (L, trunc, norm)
-        assert np.array_equal(mq.view(np.uint32), mb.view(np.uint32)), (L, trunc, norm)
+        opt = dict(want_msgs=True, rule=ginf.RULE_STANDARD, normalize=norm, store=store)
+        lq, mq = ginf.decode_hbp(P.D, P.V, synth.TRUNC_QUAD, 2, 5, **opt)
+        lb, mb = ginf.decode_hbp(P.D, P.V, synth.EXPLICIT, 2, 5, **opt)
+        case = (L, trunc, norm, store)
+        assert np.array_equal(lq, lb), case
+        assert mq.dtype == mb.dtype and np.array_equal(mq.view(np.uint8), mb.view(np.uint8)), case
 
 
 def test_wide_quadratic_lower_envelope_vs_fp64(ginf, orc):
