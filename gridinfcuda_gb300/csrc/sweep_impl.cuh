@@ -362,6 +362,65 @@ __device__ void message_std_minconv(const SweepParams &p, unsigned char *slot, i
     store_msg<T, M>(md, o, L);
 }
 
+// Two FP32 additions or subtractions in one instruction (add / sub.rn.f32x2,
+// sm_100 and later); each element is rounded exactly as the scalar operation.
+__device__ __forceinline__ uint64_t pack_f32x2(float x, float y) {
+    uint64_t v;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(v) : "f"(x), "f"(y));
+    return v;
+}
+__device__ __forceinline__ float2 unpack_f32x2(uint64_t v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ float2 add_f32x2(float ax, float ay, float bx, float by) {
+    uint64_t r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack_f32x2(ax, ay)), "l"(pack_f32x2(bx, by)));
+    return unpack_f32x2(r);
+}
+__device__ __forceinline__ float2 sub_f32x2(float ax, float ay, float bx, float by) {
+    uint64_t r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack_f32x2(ax, ay)), "l"(pack_f32x2(bx, by)));
+    return unpack_f32x2(r);
+}
+
+// The window term of output i at distance k of a quadratic message over
+// h[0, N): min(h[i-k], h[i+k]), or the one that exists at the ends.
+template <int N>
+__device__ __forceinline__ float window_pair(const float *h, int i, int k) {
+    const bool lo = i - k >= 0, hi = i + k < N;
+    if (lo && hi) return fminf(h[i - k], h[i + k]);
+    return lo ? h[i - k] : h[i + k];
+}
+
+// Outputs c .. c + B - 1 of the windowed quadratic transform over h[0, N)
+// (padded with +inf where the caller has no labels), two at a time: the
+// sums h + V(0,k) of a pair of outputs in one f32x2 addition, their minima
+// as scalars, the shift subtracted in pairs.  Values are those of the scalar
+// form below; sum accumulates the outputs in label order.
+template <int N, int QW, int B>
+__device__ __forceinline__ void window_outputs(const float *h, int c, const float *vtap, float cap, float shift,
+                                               float &sum, float *r) {
+#pragma unroll
+    for (int k = 0; k < B; k += 2) {
+        const int i = c + k;
+        const float2 t0 = add_f32x2(h[i], h[i + 1], vtap[0], vtap[0]);
+        float m0 = fminf(cap, t0.x), m1 = fminf(cap, t0.y);
+#pragma unroll
+        for (int k2 = 1; k2 <= QW; ++k2) {
+            const float2 t = add_f32x2(window_pair<N>(h, i, k2), window_pair<N>(h, i + 1, k2), vtap[k2], vtap[k2]);
+            m0 = fminf(m0, t.x);
+            m1 = fminf(m1, t.y);
+        }
+        sum += m0;
+        sum += m1;
+        const float2 o = sub_f32x2(m0, m1, shift, shift);
+        r[k] = o.x;
+        r[k + 1] = o.y;
+    }
+}
+
 // Largest truncation radius of the windowed quadratic transform (kernels are
 // compiled for radius 4 and radius 8 windows).
 constexpr int kQuadWindow = 8;
@@ -424,7 +483,11 @@ __device__ __forceinline__ void message_quad_window(const SweepParams &p, unsign
     T sum = T(0);
 #pragma unroll
     for (int c = 0; c < LMAX; c += B) {
-        if (EXACT || c < L) {
+        if constexpr (EXACT && std::is_same<T, float>::value) {
+            T r[B];
+            window_outputs<LMAX, QW, B>(h, c, vtap, cap, shift, sum, r);
+            MIO<M, T>::store(md + c * sizeof(M), r);
+        } else if (EXACT || c < L) {
             T r[B];
 #pragma unroll
             for (int k = 0; k < B; ++k) {
@@ -834,16 +897,10 @@ __device__ __forceinline__ bool tile_finish_split(const SweepParams &p, const Ta
         float sum = 0.f;
 #pragma unroll
         for (int c = 0; c < HL; c += 4) {
+            // h[QW .. QW + HL) are this half's labels; the halo (+inf off the
+            // grid of labels) lies on both sides, so no output is at an end.
             float r[4];
-#pragma unroll
-            for (int kk = 0; kk < 4; ++kk) {
-                const int ii = c + kk + QW;
-                float m = fminf(cap, h[ii] + tc.vtap[0]);
-#pragma unroll
-                for (int k2 = 1; k2 <= QW; ++k2) m = fminf(m, fminf(h[ii - k2], h[ii + k2]) + tc.vtap[k2]);
-                sum += m;
-                r[kk] = m - shift;
-            }
+            window_outputs<NH, QW, 4>(h, c + QW, tc.vtap, cap, shift, sum, r);
             MIO<float, float>::store(mh + c * sizeof(float), r);
         }
         if (hf == 0) xs.sum[g][lane] = sum;
@@ -915,8 +972,8 @@ __global__ void __launch_bounds__(NW * 32, 5) sweep_kernel_split(const SweepPara
 
 // One checkerboard half-sweep of one level: blocks take tiles in turn, each
 // issuing the copies of its next tile as soon as the current one is done.
-template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND, bool DIRECT = false>
-__global__ void __launch_bounds__(NW * 32) sweep_kernel(const SweepParams p) {
+template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND, bool DIRECT>
+__device__ __forceinline__ void sweep_body(const SweepParams &p) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t full_bar;
     // The next half-sweep may be launched now; its blocks take SM slots as
@@ -939,6 +996,21 @@ __global__ void __launch_bounds__(NW * 32) sweep_kernel(const SweepParams p) {
         if (tn < p.num_tiles) tile_load<NW>(p, tn, smem, &full_bar);
     }
     bulk_wait_all();
+}
+
+template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND, bool DIRECT = false>
+__global__ void __launch_bounds__(NW * 32) sweep_kernel(const SweepParams p) {
+    sweep_body<T, M, LMAX, EXACT, NW, KIND, DIRECT>(p);
+}
+
+// The same kernel with room for MINB blocks per SM in the register
+// allocation.  The L = 128 quadratic kernels with FP16 messages use it with
+// six (168 registers): their packed window form would otherwise take every
+// register.  (Any explicit bound, even one block, changes the allocation, so
+// the other kernels have none.)
+template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND, int MINB>
+__global__ void __launch_bounds__(NW * 32, MINB) sweep_kernel_bounded(const SweepParams p) {
+    sweep_body<T, M, LMAX, EXACT, NW, KIND, false>(p);
 }
 
 // Per-kernel launch state: the largest dynamic shared-memory size set so far
@@ -999,8 +1071,13 @@ cudaError_t launch_tiles(K kern, LaunchCache &lc_state, int NW, int nodes, const
 template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND, bool DIRECT = false>
 cudaError_t launch_one(const SweepParams &params, uint32_t slot_bytes, cudaStream_t s, int num_sms) {
     static LaunchCache cache;
-    return launch_tiles(sweep_kernel<T, M, LMAX, EXACT, NW, KIND, DIRECT>, cache, NW, NW * 8, params, slot_bytes, s,
-                        num_sms);
+    if constexpr ((KIND == KIND_QUAD || KIND == KIND_QUAD4) && sizeof(M) == 2 && LMAX == 128 && !DIRECT) {
+        return launch_tiles(sweep_kernel_bounded<T, M, LMAX, EXACT, NW, KIND, 6>, cache, NW, NW * 8, params,
+                            slot_bytes, s, num_sms);
+    } else {
+        return launch_tiles(sweep_kernel<T, M, LMAX, EXACT, NW, KIND, DIRECT>, cache, NW, NW * 8, params, slot_bytes,
+                            s, num_sms);
+    }
 }
 
 template <int NW, int QW>
