@@ -706,6 +706,8 @@ def main():
     ap.add_argument("--sweeps-per-launch", type=int, default=0,
                     help="batch workload: half-sweeps per persistent launch (0: autotuned, with --tile-nodes 0)")
     ap.add_argument("--size", default=None, help="WxH override of the workload's grid size (profiling runs)")
+    ap.add_argument("--grids", type=int, default=0,
+                    help="batch workload: number of grids (profiling runs; default 64)")
     args = ap.parse_args()
     if args.warmup < 3:
         print("note: the timing rules ask for at least 3 warm-up steps", file=sys.stderr)
@@ -713,6 +715,8 @@ def main():
     if args.size:
         w, h = (int(v) for v in args.size.lower().split("x"))
         cfg.update(W=w, H=h, name=cfg["name"].replace(f"{cfg['W']}x{cfg['H']}", f"{w}x{h}"))
+    if args.grids and args.workload == "batch":
+        cfg.update(count=args.grids, name=cfg["name"].replace(f"batch{cfg['count']}", f"batch{args.grids}"))
     if args.impl == "reference":
         run_reference(args, cfg)
     elif args.workload == "warm":
