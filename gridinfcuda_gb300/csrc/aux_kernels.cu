@@ -473,12 +473,9 @@ cudaError_t launch_icm_sync_t(const RecordFormat &f, const unsigned char *rec, i
                               const int32_t *old_labels, int32_t *new_labels, const uint8_t *chg_in, uint8_t *chg_out,
                               int *status, size_t blocks, size_t smem, cudaStream_t s) {
     auto kern = k_icm_sync<T, I, LANES>;
-    static size_t configured = 48 * 1024;
-    if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = smem;
-    }
+    static SmemLimit limit;
+    cudaError_t e = limit.ensure(kern, smem);
+    if (e != cudaSuccess) return e;
     kern<<<(unsigned)blocks, kThreads, smem, s>>>(rec, W, H, f.L, f.Lp, f.rec_bytes, static_cast<const T *>(V),
                                                    old_labels, new_labels, chg_in, chg_out, status);
     return cudaGetLastError();
@@ -798,12 +795,9 @@ cudaError_t launch_pyr_lp_t(const Tin *src, int W, int H, int L, unsigned char *
                             uint32_t rec_bytes, cudaStream_t s) {
     auto kern = k_costs_to_records_pyr_lp<Tin, T, LP, XC>;
     const size_t smem = (size_t)2 * LP * (XC + 1) * sizeof(T);
-    static bool configured = false;
-    if (!configured && smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    static SmemLimit limit;
+    cudaError_t e = limit.ensure(kern, smem);
+    if (e != cudaSuccess) return e;
     const dim3 grid((W + XC - 1) / XC, (unsigned)std::min((H + 1) / 2, 65535));
     kern<<<grid, 256, smem, s>>>(src, W, H, L, rec, crec, cW, rec_bytes);
     return cudaGetLastError();
@@ -905,25 +899,23 @@ cudaError_t launch_export_messages(const RecordFormat &f, const unsigned char *r
 // it exceeds the default 48 KB.
 template <typename K>
 cudaError_t icm_smem_attr(K kern, size_t bytes) {
-    static size_t configured = 48 * 1024;
-    if (bytes > configured) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-        if (e != cudaSuccess) return e;
-        configured = bytes;
-    }
-    return cudaSuccess;
+    static SmemLimit limit;
+    return limit.ensure(kern, bytes);
 }
 
-int g_num_sms = 0;
-
+// SM count of the current device (memoised per device; a failed query is
+// not remembered).
 int num_sms() {
-    if (g_num_sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_num_sms <= 0) g_num_sms = 1;
+    static std::atomic<int> count[kMaxDevices];
+    const int dev = current_device();
+    int n = count[dev].load(std::memory_order_relaxed);
+    if (n > 0) return n;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        return 1;
     }
-    return g_num_sms;
+    count[dev].store(n, std::memory_order_relaxed);
+    return n;
 }
 
 cudaError_t launch_icm_sync(const RecordFormat &f, const unsigned char *rec, int W, int H, const void *V,

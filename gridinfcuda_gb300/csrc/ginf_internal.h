@@ -14,8 +14,10 @@
 // every slot is a whole number of 16-byte chunks for f16, f32, i32 and f64.
 #pragma once
 
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
+#include <mutex>
 
 #include <cuda_runtime.h>
 
@@ -64,6 +66,56 @@ struct SweepParams {
     int tiles_per_row, num_tiles;  // set by the launcher for the variant it runs
     int quad_radius;               // truncation radius of a quadratic table (kernel choice only)
     int *status;
+};
+
+// Per-kernel launch state kept across calls, safe for concurrent host
+// threads and separate per device (kernel attributes and occupancy belong to
+// a device).  Instances live in static storage, where the atomics start at 0.
+constexpr int kMaxDevices = 64;
+
+inline int current_device() {
+    int d = 0;
+    if (cudaGetDevice(&d) != cudaSuccess) return 0;
+    return d >= 0 && d < kMaxDevices ? d : 0;
+}
+
+// The dynamic shared memory a kernel may use: raised on a device, under a
+// lock and only ever upward, the first time a launch needs more than the
+// default 48 KB or than allowed so far.
+struct SmemLimit {
+    std::atomic<size_t> allowed[kMaxDevices];
+    std::mutex lock;
+    template <typename K>
+    cudaError_t ensure(K kern, size_t bytes) {
+        if (bytes <= 48 * 1024) return cudaSuccess;
+        std::atomic<size_t> &a = allowed[current_device()];
+        if (bytes <= a.load(std::memory_order_acquire)) return cudaSuccess;
+        std::lock_guard<std::mutex> g(lock);
+        if (bytes <= a.load(std::memory_order_relaxed)) return cudaSuccess;
+        const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (e == cudaSuccess) a.store(bytes, std::memory_order_release);
+        return e;
+    }
+};
+
+// Resident blocks per SM of a kernel at a given dynamic shared memory size:
+// the last answer per device, kept as one word (size + 1 in the high half,
+// blocks in the low half) so readers never see a torn pair.
+struct OccupancyMemo {
+    std::atomic<uint64_t> last[kMaxDevices];
+    template <typename K>
+    cudaError_t blocks(K kern, int threads, size_t smem, int &occ) {
+        std::atomic<uint64_t> &a = last[current_device()];
+        const uint64_t key = (uint64_t)(smem + 1) << 32;
+        const uint64_t v = a.load(std::memory_order_relaxed);
+        if ((v & ~0xffffffffull) == key) {
+            occ = (int)(uint32_t)v;
+            return cudaSuccess;
+        }
+        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, smem);
+        if (e == cudaSuccess) a.store(key | (uint32_t)occ, std::memory_order_relaxed);
+        return e;
+    }
 };
 
 // Nodes per sweep tile (8, 16 or 32; 16 unless a tuned choice says otherwise).

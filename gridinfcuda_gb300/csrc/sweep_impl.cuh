@@ -1013,11 +1013,10 @@ __global__ void __launch_bounds__(NW * 32, MINB) sweep_kernel_bounded(const Swee
     sweep_body<T, M, LMAX, EXACT, NW, KIND, false>(p);
 }
 
-// Per-kernel launch state: the largest dynamic shared-memory size set so far
-// and the occupancy last computed.
+// Per-kernel launch state (one per kernel instantiation, in static storage).
 struct LaunchCache {
-    size_t configured = 0;
-    int occ_smem = -1, occ = 0;
+    SmemLimit smem;
+    OccupancyMemo occ;
 };
 
 // Launches one half-sweep kernel over tiles of `nodes` nodes, NW warps per
@@ -1033,22 +1032,11 @@ cudaError_t launch_tiles(K kern, LaunchCache &lc_state, int NW, int nodes, const
     p.num_tiles = p.H >= 3 ? (p.H - 2) * p.tiles_per_row : 0;
     if (p.num_tiles <= 0) return cudaSuccess;
     const size_t smem = (size_t)nodes * slot_bytes;
-    size_t &configured = lc_state.configured;
-    int &occ_cache_smem = lc_state.occ_smem, &occ_cache = lc_state.occ;
-    if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = smem;
-    }
+    cudaError_t e = lc_state.smem.ensure(kern, smem);
+    if (e != cudaSuccess) return e;
     int occ = 0;
-    if (occ_cache_smem == (int)smem) {
-        occ = occ_cache;
-    } else {
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NW * 32, smem);
-        if (e != cudaSuccess) return e;
-        occ_cache_smem = (int)smem;
-        occ_cache = occ;
-    }
+    e = lc_state.occ.blocks(kern, NW * 32, smem, occ);
+    if (e != cudaSuccess) return e;
     if (occ < 1) return cudaErrorInvalidConfiguration;
     int grid = occ * num_sms;
     if (grid > p.num_tiles) grid = p.num_tiles;
