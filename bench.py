@@ -297,7 +297,7 @@ def run_ours(args, cfg):
     traffic = load_traffic(cfg)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-                "kernel": "sweep_kernel<float,float,64,...> (finest level)",
+                "kernel": f"sweep_kernel<float,float,{L},...> (finest level)",
                 "algorithmic_bytes_per_launch": alg_bytes, "mean_launch_ms": round(per_launch_s * 1e3, 4),
                 "launches_per_step": l0_launches}
 

@@ -322,6 +322,46 @@ def test_stream_ordered_solve(ginf):
         w.close()
 
 
+def test_concurrent_host_threads(ginf):
+    """Calls are reentrant per workspace: four host threads, each with its own
+    workspace and stream, solve different grids (label counts 16, 24, 64 and
+    128, so several kernels and their launch caches are first used
+    concurrently) at the same time; every result equals the single-thread
+    call."""
+    import threading
+    import torch
+    cases = [synth.random_problem(90 + 7 * k, 70 + 5 * k, L, 300 + k, model=synth.TRUNC_QUAD if L == 24 else
+                                  synth.TRUNC_LINEAR) for k, L in enumerate((16, 24, 64, 128))]
+    got = [None] * len(cases)
+    errors = []
+    start = threading.Barrier(len(cases))
+
+    def run(k):
+        try:
+            P = cases[k]
+            stream = torch.cuda.Stream()
+            with ginf.Workspace() as ws:
+                start.wait()
+                res = []
+                for _ in range(3):
+                    res.append(ginf.solve(P.D, P.V, P.model, 3, 5, 2, workspace=ws, stream=stream.cuda_stream))
+                got[k] = res
+        except Exception as e:  # reported on the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=run, args=(k,)) for k in range(len(cases))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    want = [ginf.solve(P.D, P.V, P.model, 3, 5, 2) for P in cases]
+    for k, res in enumerate(got):
+        for lab, e in res:
+            assert np.array_equal(lab[1:-1, 1:-1], want[k][0][1:-1, 1:-1]), k
+            assert e == want[k][1], k
+
+
 @pytest.mark.parametrize("W,H", [(1, 1), (2, 9), (9, 2), (1, 40), (3, 3), (4, 3)])
 def test_grids_without_or_with_tiny_interior(ginf, orc, W, H):
     """Grids with no interior node (nothing updates: every label stays the
