@@ -3,7 +3,8 @@
 //
 // Every wait here is bounded: after kWaitLimitNs of wall time (read from
 // %globaltimer) it records DEV_ERR_TIMEOUT in the launch's status word and
-// returns false, so a kernel can never spin forever.
+// returns false (an mbarrier wait first gives its copies the same time again
+// to land), so a kernel can never spin forever.
 #pragma once
 
 #include <cstdint>
@@ -51,15 +52,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Waits for the barrier phase with the given parity; false after the time limit.
+// Waits for the barrier phase with the given parity.  After the time limit
+// it records DEV_ERR_TIMEOUT and keeps waiting, for at most the same time
+// again, so that copies still in flight land before the caller gives up and
+// its shared memory is released; it then returns false, whether or not the
+// phase completed in that second period.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *status) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = global_timer_ns();
+    bool late = false;
     for (uint32_t n = 1;; ++n) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if ((n & 63u) == 0 && global_timer_ns() - t0 > kWaitLimitNs) {
-            if (status) atomicOr(status, DEV_ERR_TIMEOUT);
-            return false;
+        if (mbar_try_wait(bar, parity)) return !late;
+        if ((n & 63u) == 0) {
+            const uint64_t dt = global_timer_ns() - t0;
+            if (!late && dt > kWaitLimitNs) {
+                if (status) atomicOr(status, DEV_ERR_TIMEOUT);
+                late = true;
+            }
+            if (dt > 2 * kWaitLimitNs) return false;
         }
     }
 }
