@@ -385,6 +385,14 @@ __device__ __forceinline__ float2 sub_f32x2(float ax, float ay, float bx, float 
     return unpack_f32x2(r);
 }
 
+// Minimum of three FP32 values in one instruction (three-input min.f32,
+// sm_100 and later); exact, like the two-input minimum.
+__device__ __forceinline__ float min3_f32(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
 // The window term of output i at distance k of a quadratic message over
 // h[0, N): min(h[i-k], h[i+k]), or the one that exists at the ends.
 template <int N>
@@ -406,12 +414,24 @@ __device__ __forceinline__ void window_outputs(const float *h, int c, const floa
     for (int k = 0; k < B; k += 2) {
         const int i = c + k;
         const float2 t0 = add_f32x2(h[i], h[i + 1], vtap[0], vtap[0]);
-        float m0 = fminf(cap, t0.x), m1 = fminf(cap, t0.y);
+        float a0[QW + 1], a1[QW + 1];
 #pragma unroll
         for (int k2 = 1; k2 <= QW; ++k2) {
             const float2 t = add_f32x2(window_pair<N>(h, i, k2), window_pair<N>(h, i + 1, k2), vtap[k2], vtap[k2]);
-            m0 = fminf(m0, t.x);
-            m1 = fminf(m1, t.y);
+            a0[k2] = t.x;
+            a1[k2] = t.y;
+        }
+        // The minimum over {cap, h + V(0,0), the QW window terms}, three at a time.
+        float m0 = min3_f32(cap, t0.x, a0[1]), m1 = min3_f32(cap, t0.y, a1[1]);
+#pragma unroll
+        for (int k2 = 2; k2 <= QW; k2 += 2) {
+            if (k2 + 1 <= QW) {
+                m0 = min3_f32(m0, a0[k2], a0[k2 + 1]);
+                m1 = min3_f32(m1, a1[k2], a1[k2 + 1]);
+            } else {
+                m0 = fminf(m0, a0[k2]);
+                m1 = fminf(m1, a1[k2]);
+            }
         }
         sum += m0;
         sum += m1;
