@@ -1116,15 +1116,17 @@ ginf_status ginf_stereo_costs(int32_t width, int32_t height, int32_t num_labels,
     const size_t img = (size_t)width * height * sizeof(float);
     const float *l = left, *r = right;
     float *tmp = nullptr;
+    cudaError_t e = cudaSuccess;
     if (memory == GINF_HOST) {
         GINF_CK(cudaMallocAsync(&tmp, 2 * img, s));
-        GINF_CK(cudaMemcpyAsync(tmp, left, img, cudaMemcpyHostToDevice, s));
-        GINF_CK(cudaMemcpyAsync(tmp + (size_t)width * height, right, img, cudaMemcpyHostToDevice, s));
+        e = cudaMemcpyAsync(tmp, left, img, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(tmp + (size_t)width * height, right, img, cudaMemcpyHostToDevice, s);
         l = tmp;
         r = tmp + (size_t)width * height;
     }
-    cudaError_t e = launch_stereo_costs(width, height, num_labels, l, r, coef, cap, costs, s);
-    if (tmp) cudaFreeAsync(tmp, s);
+    if (e == cudaSuccess) e = launch_stereo_costs(width, height, num_labels, l, r, coef, cap, costs, s);
+    if (tmp) cudaFreeAsync(tmp, s);  // stream-ordered: after the copies and the kernel
     if (e != cudaSuccess) return cuda_fail(e, "stereo costs");
     GINF_CK(cudaStreamSynchronize(s));
     return GINF_OK;
