@@ -94,10 +94,15 @@ namespace {
 
 enum { EV_START, EV_UPLOAD, EV_PREPARE, EV_L0_START, EV_SWEEPS, EV_ICM, EV_ENERGY, EV_END, EV_COUNT };
 
+// A workspace belongs to the device of its first call: its buffers and
+// events live there, so calls from another device are refused.
 ginf_status check_device(ginf_workspace *ws) {
     int dev = 0;
     GINF_CK(cudaGetDevice(&dev));
     if (ws->device == dev) return GINF_OK;
+    if (ws->device >= 0)
+        return fail(GINF_ERR_INVALID_ARGUMENT, "workspace belongs to device " + std::to_string(ws->device) +
+                                                   ", the calling thread's current device is " + std::to_string(dev));
     cudaDeviceProp prop;
     cudaError_t e = cudaGetDeviceProperties(&prop, dev);
     if (e != cudaSuccess) return fail(GINF_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));

@@ -136,9 +136,11 @@ const char *ginf_version(void);
 const char *ginf_last_error(void);
 void ginf_default_options(ginf_options *opt);
 
-/* Reusable device buffers and events; one per host thread or stream.
- * Passing NULL to the solver entry points allocates and frees per call, as
- * the reference does (src/gpu/bp.cu:141-222). */
+/* Reusable device buffers and events; one per host thread or stream.  A
+ * workspace belongs to the device that is current at its first call; calls
+ * from another device return GINF_ERR_INVALID_ARGUMENT.  Passing NULL to the
+ * solver entry points allocates and frees per call, as the reference does
+ * (src/gpu/bp.cu:141-222). */
 ginf_status ginf_workspace_create(ginf_workspace **ws);
 ginf_status ginf_workspace_destroy(ginf_workspace *ws);
 /* Waits for the workspace's stream-ordered calls and reports a device-side
