@@ -256,6 +256,7 @@ struct BatchGroup {
 };
 
 struct ginf_batch {
+    int device = -1;  // the device the plan was built on (its buffers and graph live there)
     int count = 0, iters = 0;
     std::vector<ginf_grid> grids;
     std::vector<int32_t *> labels;
@@ -555,6 +556,7 @@ ginf_status ginf_batch_create(ginf_batch **out, const ginf_grid *grids, int32_t 
     if (!coop) return bfail(GINF_ERR_NO_DEVICE, "the device does not support cooperative launches");
 
     ginf_batch *b = new ginf_batch();
+    b->device = dev;
     b->count = count;
     b->iters = iters;
     b->grids.assign(grids, grids + count);
@@ -655,9 +657,25 @@ ginf_status batch_enter(ginf_batch *b, cudaStream_t s) {
 
 }  // namespace
 
+namespace {
+// A plan replays only on the device it was built on.
+ginf_status check_batch_device(const ginf_batch *b) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return bfail(GINF_ERR_NO_DEVICE, "no current CUDA device");
+    }
+    if (dev != b->device)
+        return bfail(GINF_ERR_INVALID_ARGUMENT, "batch was built on device " + std::to_string(b->device) +
+                                                    ", the calling thread's current device is " + std::to_string(dev));
+    return GINF_OK;
+}
+}  // namespace
+
 ginf_status ginf_batch_enqueue(ginf_batch *b, void *stream) {
     ginf_gpu::set_last_error("");
     if (!b || !b->exec) return bfail(GINF_ERR_INVALID_ARGUMENT, "batch is NULL or has no captured solve");
+    if (ginf_status st = check_batch_device(b); st != GINF_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     ginf_status st = batch_enter(b, s);
     if (st != GINF_OK) return st;
@@ -682,6 +700,7 @@ ginf_status ginf_batch_sync(ginf_batch *b) {
 ginf_status ginf_batch_run(ginf_batch *b, void *stream, ginf_stats *stats) {
     ginf_gpu::set_last_error("");
     if (!b || !b->exec) return bfail(GINF_ERR_INVALID_ARGUMENT, "batch is NULL or has no captured solve");
+    if (ginf_status st = check_batch_device(b); st != GINF_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     {
         ginf_status st = batch_enter(b, s);

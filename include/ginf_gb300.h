@@ -203,7 +203,9 @@ ginf_status ginf_stereo_costs(int32_t width, int32_t height, int32_t num_labels,
  * the autotuner, which times the candidates on this batch and caches the
  * winner per mix of (label count, log2 node count) buckets in the JSON file
  * named by $GINF_AUTOTUNE_CACHE (default
- * $XDG_CACHE_HOME or ~/.cache/gridinfcuda_gb300_autotune.json). */
+ * $XDG_CACHE_HOME or ~/.cache/gridinfcuda_gb300_autotune.json).  A plan
+ * runs only on the device current at its creation; runs from another device
+ * return GINF_ERR_INVALID_ARGUMENT. */
 typedef struct ginf_batch ginf_batch;
 ginf_status ginf_batch_create(ginf_batch **batch, const ginf_grid *grids, int32_t *const *labels, int32_t count,
                               int32_t iters, const ginf_options *opt);
