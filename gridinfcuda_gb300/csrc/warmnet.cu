@@ -320,6 +320,7 @@ using namespace ginf_gpu;
 // The network object.
 
 struct ginf_warmnet {
+    int device = -1;  // the device its parameters and buffers live on
     int L = 0, hidden = 0;
     int cin[4], cout[4];
     size_t woff[4], boff[4], nparams = 0;  // offsets into the flat FP32 parameter vector
@@ -511,6 +512,11 @@ ginf_status backward(ginf_warmnet *n, const float *target, Geo g, cudaStream_t s
 ginf_status check_geo(const ginf_warmnet *n, int nimg, int h, int w) {
     if (!n) return wfail(GINF_ERR_INVALID_ARGUMENT, "warmnet is NULL");
     if (nimg < 1 || h < 1 || w < 1) return wfail(GINF_ERR_INVALID_ARGUMENT, "bad batch geometry");
+    int dev = 0;
+    GINF_WCK(cudaGetDevice(&dev));
+    if (dev != n->device)
+        return wfail(GINF_ERR_INVALID_ARGUMENT, "network was created on device " + std::to_string(n->device) +
+                                                    ", the calling thread's current device is " + std::to_string(dev));
     return GINF_OK;
 }
 
@@ -544,7 +550,8 @@ ginf_status ginf_warmnet_create(ginf_warmnet **out, int32_t num_labels, int32_t 
     n->L = num_labels;
     n->hidden = hidden;
     layout(n);
-    ginf_status st = alloc_params(n);
+    ginf_status st = cudaGetDevice(&n->device) == cudaSuccess ? alloc_params(n)
+                                                               : wfail(GINF_ERR_NO_DEVICE, "no current CUDA device");
     if (st != GINF_OK) {
         ginf_warmnet_destroy(n);
         return st;
