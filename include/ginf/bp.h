@@ -10,6 +10,13 @@
 
 #include "core.h"
 
+// Thread-block shape of the reference's GPU BP kernels (32 x 4).  Kept so
+// code written against the reference keeps compiling; this library's sweep
+// kernels choose their own tiles (8, 16 or 32 same-colour nodes of a row) and
+// do not read these values.
+#define GINF_BP_BLOCK_WIDTH 32
+#define GINF_BP_BLOCK_HEIGHT 4
+
 namespace ginf {
 
 template <typename T>

@@ -7,6 +7,11 @@
 
 #include "core.h"
 
+// Thread-block side of the reference's GPU ICM kernel (16 x 16).  Kept so
+// code written against the reference keeps compiling; this library's ICM
+// kernels use lanes per node and do not read it.
+#define GINF_ICM_BLOCK_SIZE 16
+
 namespace ginf {
 
 // Synchronous (Jacobi) sweeps: every node reads the previous sweep's labels.

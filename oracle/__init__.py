@@ -21,7 +21,22 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libginf_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libginf_ref.so")
-REF_SRC = "/root/reference"
+
+
+def _reference_dir() -> str:
+    """Where the reference checkout is looked for: $GINF_REFERENCE, else the
+    default that oracle/Makefile holds (the one recipe naming a location)."""
+    env = os.environ.get("GINF_REFERENCE")
+    if env:
+        return env
+    try:
+        r = subprocess.run(["make", "-s", "-C", HERE, "ref-dir"], capture_output=True, text=True, timeout=30)
+        return r.stdout.strip()
+    except Exception:
+        return ""
+
+
+REF_SRC = _reference_dir()
 
 _i = ctypes.c_int
 _p = ctypes.c_void_p
@@ -33,7 +48,7 @@ def build(with_ref: bool | None = None) -> None:
     """Compile the oracle; also the reference bridge when its sources exist."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
     if with_ref is None:
-        with_ref = os.path.isdir(os.path.join(REF_SRC, "src"))
+        with_ref = bool(REF_SRC) and os.path.isdir(os.path.join(REF_SRC, "src"))
     if with_ref:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
 

@@ -20,6 +20,11 @@
 #include "ginf/core.h"
 #include "ginf/icm.h"
 
+// Reference code may size its own buffers or launches with the library's
+// block-shape macros (src/include/bp.h:8-9, icm.h:8); they stay defined.
+static_assert(GINF_BP_BLOCK_WIDTH * GINF_BP_BLOCK_HEIGHT == 128 && GINF_ICM_BLOCK_SIZE == 16,
+              "reference block-shape macros");
+
 int main(int argc, char **argv) {
     if (argc != 3) {
         std::fprintf(stderr, "usage: %s in.raw out.raw\n", argv[0]);

@@ -122,3 +122,40 @@ def test_option_and_entry_point_validation_without_device(built_lib):
     assert L.ginf_workspace_sync(None) == capi.ERR_INVALID_ARGUMENT
     # the bounded-wait self-test needs its output pointers
     assert L.ginf_selftest_bounded_waits(None, None) == capi.ERR_INVALID_ARGUMENT
+
+
+MACRO_PROGRAM = r'''
+#include "ginf/core.h"
+#include "ginf/bp.h"
+#include "ginf/icm.h"
+// Every macro, enum and constant the reference's public headers define
+// (src/include/{utils,matrix,bp,icm}.h), with the reference's values.
+static_assert(GINF_BP_BLOCK_WIDTH == 32 && GINF_BP_BLOCK_HEIGHT == 4, "bp.h:8-9");
+static_assert(GINF_ICM_BLOCK_SIZE == 16, "icm.h:8");
+static_assert(GINF_MAT_MAX_NUM_DIMS == 4, "matrix.h:6");
+static_assert(GINF_UNDEFINED == -1 && GINF_NUM_DIR == 4, "utils.h:4-7");
+static_assert(GINF_OPP_DIR(ginf::GINF_DIR_S) == ginf::GINF_DIR_N && GINF_OPP_DIR(ginf::GINF_DIR_W) == ginf::GINF_DIR_E,
+              "utils.h:10");
+static_assert(GINF_IS_VALID_NODE(0, 0, 1, 1) && !GINF_IS_VALID_NODE(1, 0, 1, 1), "utils.h:13");
+static_assert(GINF_MIN(3, 4) == 3 && GINF_MAX(3, 4) == 4 && GINF_ABS(-5) == 5 && GINF_SQ(-3) == 9, "utils.h:16-19");
+static_assert(GINF_MAX_NUM_LABELS >= 16, "utils.h:22 (raised to 128 here)");
+static_assert(ginf::GINF_SM_EXPLICIT == 0 && ginf::GINF_SM_TRUNC_QUAD == 3, "grid.h:9-14");
+int main() {
+    int block[2] = {GINF_BP_BLOCK_WIDTH, GINF_BP_BLOCK_HEIGHT};
+    int s = 0;
+    for (int d = 0; d < GINF_NUM_DIR; ++d) s += ginf::dirX[d] * 10 + ginf::dirY[d];
+    return (s == 0 && block[0] * block[1] == 128 && GINF_ICM_BLOCK_SIZE * GINF_ICM_BLOCK_SIZE == 256) ? 0 : 1;
+}
+'''
+
+
+def test_reference_macros_compile_against_headers(tmp_path):
+    """User code that uses the reference headers' macros (the BP / ICM block
+    sizes included) compiles against include/ginf and sees the same values."""
+    src = tmp_path / "macros.cc"
+    src.write_text(MACRO_PROGRAM)
+    exe = tmp_path / "macros"
+    r = subprocess.run(["g++", "-std=c++17", "-I" + os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert subprocess.run([str(exe)]).returncode == 0

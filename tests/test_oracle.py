@@ -52,7 +52,7 @@ def test_oracle_stereo_png_vs_reference(orc):
     import os
     import struct
     import zlib
-    path = "/root/reference/examples/stereo"
+    path = os.path.join(orc.REF_SRC, "examples", "stereo")
 
     def gray(png):
         data = open(png, "rb").read()
