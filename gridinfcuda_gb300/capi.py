@@ -85,6 +85,7 @@ def lib():
         L.ginf_solve.argtypes = [_p, ctypes.POINTER(Grid), _i32, _i32, _i32, _p, ctypes.POINTER(ctypes.c_double),
                                  ctypes.POINTER(Options), ctypes.POINTER(Stats)]
         L.ginf_stereo_costs.argtypes = [_i32, _i32, _i32, _i32, _p, _p, ctypes.c_float, ctypes.c_float, _p, _p]
+        L.ginf_stereo_costs_u8.argtypes = [_i32, _i32, _i32, _i32, _p, _p, _i32, _p, _p]
         L.ginf_batch_create.argtypes = [ctypes.POINTER(_p), ctypes.POINTER(Grid), ctypes.POINTER(_p), _i32, _i32,
                                         ctypes.POINTER(Options)]
         L.ginf_batch_run.argtypes = [_p, _p, ctypes.POINTER(Stats)]
@@ -113,6 +114,7 @@ def lib():
         L.ginf_decode_hbp_warm.argtypes = [_p, ctypes.POINTER(Grid), _i32, _i32, _i32, _i32, _i32, _p, _i32, _p,
                                            ctypes.POINTER(Options), ctypes.POINTER(Stats)]
         for name in ("ginf_decode_hbp", "ginf_decode_icm", "ginf_energy", "ginf_solve", "ginf_stereo_costs",
+                     "ginf_stereo_costs_u8",
                      "ginf_workspace_create", "ginf_workspace_destroy", "ginf_batch_create", "ginf_batch_run",
                      "ginf_batch_config", "ginf_batch_destroy", "ginf_decode_bp_batch", "ginf_warmnet_create",
                      "ginf_warmnet_load", "ginf_warmnet_save", "ginf_warmnet_destroy", "ginf_warmnet_num_params",
@@ -301,6 +303,19 @@ def stereo_costs(left, right, L, coef, cap, out, stream=None):
     if om != DEVICE:
         raise ValueError("out must be a CUDA tensor")
     check(lib().ginf_stereo_costs(W, H, L, lm, lp, rp, coef, cap, op, stream))
+    return out
+
+
+def stereo_costs_u8(left, right, L, cap, out, stream=None):
+    """The reference example's integer cost volume (examples/stereo/stereo.cc:28-34)
+    from 8-bit grey images into the CUDA int32 tensor ``out`` (L, H, W)."""
+    H, W = left.shape
+    lp, lm = _ptr(left)
+    rp, _ = _ptr(right)
+    op, om = _ptr(out)
+    if om != DEVICE:
+        raise ValueError("out must be a CUDA tensor")
+    check(lib().ginf_stereo_costs_u8(W, H, L, lm, lp, rp, cap, op, stream))
     return out
 
 

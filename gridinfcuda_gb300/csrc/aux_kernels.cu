@@ -631,6 +631,27 @@ __global__ void k_stereo_costs(int W, int H, int L, const float *__restrict__ le
     costs[idx] = coef * fminf(fabsf(a - b), cap);
 }
 
+// The reference example's integer recipe (examples/stereo/stereo.cc:28-34):
+// for x >= L-1, D(x, y, k) = min(|left(x,y) - right(x-k,y)|, cap) on 8-bit
+// grey images; the columns x < L-1 keep zero cost (the Grid constructor's
+// zero fill, src/matrix.cc:21-27).  One thread per cost element, label-planar.
+__global__ void k_stereo_costs_u8(int W, int H, int L, const uint8_t *__restrict__ left,
+                                  const uint8_t *__restrict__ right, int cap, int32_t *__restrict__ costs) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t total = (size_t)W * H * L;
+    if (idx >= total) return;
+    const int x = (int)(idx % W);
+    const int y = (int)((idx / W) % H);
+    const int k = (int)(idx / ((size_t)W * H));
+    int c = 0;
+    if (x >= L - 1) {
+        const int a = left[(size_t)y * W + x];
+        const int b = right[(size_t)y * W + x - k];
+        c = min(abs(a - b), cap);
+    }
+    costs[idx] = c;
+}
+
 // Level-t inputs and targets of the warm-start network (FP32 records):
 // costs and beliefs per fine node, i.e. divided by scale = 4^t.
 __global__ void k_level_x(const unsigned char *__restrict__ rec, int W, int H, int L, uint32_t rec_bytes, float scale,
@@ -1053,6 +1074,13 @@ cudaError_t launch_stereo_costs(int W, int H, int L, const float *left, const fl
                                 float *costs, cudaStream_t s) {
     const size_t total = (size_t)W * H * L;
     k_stereo_costs<<<blocks_for(total), kThreads, 0, s>>>(W, H, L, left, right, coef, cap, costs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stereo_costs_u8(int W, int H, int L, const uint8_t *left, const uint8_t *right, int cap,
+                                   int32_t *costs, cudaStream_t s) {
+    const size_t total = (size_t)W * H * L;
+    k_stereo_costs_u8<<<blocks_for(total), kThreads, 0, s>>>(W, H, L, left, right, cap, costs);
     return cudaGetLastError();
 }
 

@@ -1137,4 +1137,30 @@ ginf_status ginf_stereo_costs(int32_t width, int32_t height, int32_t num_labels,
     return GINF_OK;
 }
 
+ginf_status ginf_stereo_costs_u8(int32_t width, int32_t height, int32_t num_labels, int32_t memory,
+                                 const uint8_t *left, const uint8_t *right, int32_t cap, int32_t *costs,
+                                 void *stream) {
+    g_last_error.clear();
+    if (width < 1 || height < 1 || num_labels < 1) return fail(GINF_ERR_INVALID_ARGUMENT, "bad size");
+    if (!left || !right || !costs) return fail(GINF_ERR_INVALID_ARGUMENT, "NULL buffer");
+    if (memory != GINF_HOST && memory != GINF_DEVICE) return fail(GINF_ERR_INVALID_ARGUMENT, "bad memory kind");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t img = (size_t)width * height;
+    const uint8_t *l = left, *r = right;
+    uint8_t *tmp = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (memory == GINF_HOST) {
+        GINF_CK(cudaMallocAsync(&tmp, 2 * img, s));
+        e = cudaMemcpyAsync(tmp, left, img, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(tmp + img, right, img, cudaMemcpyHostToDevice, s);
+        l = tmp;
+        r = tmp + img;
+    }
+    if (e == cudaSuccess) e = launch_stereo_costs_u8(width, height, num_labels, l, r, cap, costs, s);
+    if (tmp) cudaFreeAsync(tmp, s);
+    if (e != cudaSuccess) return cuda_fail(e, "stereo costs");
+    GINF_CK(cudaStreamSynchronize(s));
+    return GINF_OK;
+}
+
 }  // extern "C"

@@ -178,5 +178,7 @@ void set_last_error(const char *msg);
 
 cudaError_t launch_stereo_costs(int W, int H, int L, const float *left, const float *right, float coef, float cap,
                                 float *costs, cudaStream_t s);
+cudaError_t launch_stereo_costs_u8(int W, int H, int L, const uint8_t *left, const uint8_t *right, int cap,
+                                   int32_t *costs, cudaStream_t s);
 
 }  // namespace ginf_gpu

@@ -40,7 +40,9 @@ DeviceSetup g_setup[kMaxDevices];
 
 // Host code cannot use g_noalloc_scratch directly (in host code the name is
 // only a stand-in); its device address comes from cudaGetSymbolAddress, once
-// per device, with that device current.
+// per device, with that device current.  The address is kept for the life of
+// the process: a cudaDeviceReset on that device after the first call would
+// leave it stale (the header says so).
 ginf_status setup_device(int dev, DeviceSetup &out) {
     if (dev < 0 || dev >= kMaxDevices) {
         ginf_gpu::set_last_error("ginf_decode_bp_noalloc: device ordinal out of range");

@@ -190,6 +190,19 @@ ginf_status ginf_stereo_costs(int32_t width, int32_t height, int32_t num_labels,
                               const float *left, const float *right, float coef, float cap,
                               float *costs, void *stream);
 
+/* Stereo data costs by the reference example's own integer recipe
+ * (examples/stereo/stereo.cc:28-34), on the device: for every column
+ * x >= L-1, D(x, y, k) = min(|left(x,y) - right(x-k,y)|, cap) for k < L;
+ * columns x < L-1 get zero cost, as the reference's zero-initialised grid
+ * leaves them.  left / right are W*H 8-bit grey images (the example's
+ * CV_LOAD_IMAGE_GRAYSCALE matrices) in the memory kind given; costs is
+ * int32, label-planar, device memory (W*H*L), ready for a GINF_I32 grid.
+ * The example uses L = 16 and cap = 20, then TruncLinear(10, 20) and 30
+ * iterations of gpuDecodeBp. */
+ginf_status ginf_stereo_costs_u8(int32_t width, int32_t height, int32_t num_labels, int32_t memory,
+                                 const uint8_t *left, const uint8_t *right, int32_t cap, int32_t *costs,
+                                 void *stream);
+
 /* Batches: many independent grids, each solved by loopy BP (one level,
  * `iters` half-sweeps, the reference's semantics and stale-belief decode, as
  * ginf_decode_hbp with num_levels == 1).  The reference solves one grid per
@@ -303,13 +316,18 @@ ginf_status ginf_decode_hbp_warm(ginf_workspace *ws, const ginf_grid *grid, int3
  * ginf_decode_hbp; the working set (the message records and a status word)
  * lives in one fixed array of GINF_NOALLOC_SCRATCH_BYTES in the library's
  * device image, which every GPU that loads the library holds until the
- * process exits.  Grids needing more than that (about
- * GINF_NOALLOC_SCRATCH_BYTES / (20 * L) nodes for FP32 / int32) are rejected
- * with GINF_ERR_INVALID_ARGUMENT.  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  All calls share the
- * array: calls whose work overlaps on the GPU race and must be serialised by
- * the caller.  The call synchronises `stream` (a cudaStream_t, NULL = legacy
+ * process exits.  A W x H grid with L labels needs exactly
+ *     256 + W * H * 20 * Lp  bytes,   Lp = L rounded up to a multiple of 8
+ * (one record of 5 * Lp four-byte elements per node -- its costs and four
+ * incoming messages -- after a 256-byte status block), for FP32 and int32
+ * alike; grids needing more than GINF_NOALLOC_SCRATCH_BYTES are rejected with
+ * GINF_ERR_INVALID_ARGUMENT and nothing runs.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current and keeps it for the process; make that first call before any
+ * stream capture, and do not call cudaDeviceReset on that device afterwards
+ * (a new context may place the array elsewhere).  All calls share the array:
+ * calls whose work overlaps on the GPU race and must be serialised by the
+ * caller.  The call synchronises `stream` (a cudaStream_t, NULL = legacy
  * default stream) before it returns. */
 #define GINF_NOALLOC_SCRATCH_BYTES (48u * 1024u * 1024u)
 ginf_status ginf_decode_bp_noalloc(const ginf_grid *grid, int32_t num_iters, int32_t *labels, void *stream);

@@ -28,6 +28,7 @@ sys.path.insert(0, ROOT)
 
 import oracle  # noqa: E402
 from gridinfcuda_gb300 import synth  # noqa: E402
+from png_grey import grey, stereo_costs_u8  # noqa: E402
 
 
 def sha(a: np.ndarray) -> str:
@@ -73,14 +74,49 @@ def initial_labels(W, H, L, seed):
     return rng.integers(0, L - 1, W * H).reshape(H, W).astype(np.int32)
 
 
+def stereo_png_case(gold, arrays):
+    """The reference example end to end (examples/stereo/stereo.cc:16-43):
+    its own stereo pair as grey images, Grid<int> with L = 16 and costs
+    min(|left(x) - right(x-k)|, 20) for x >= L-1, TruncLinear(10, 20), 30
+    iterations of loopy BP by the reference's CPU code.  The grey images are
+    stored (the GPU test has no reference checkout), the labels both as an
+    array and as a SHA-256."""
+    path = os.path.join(oracle.REF_SRC, "examples", "stereo")
+    left, right = grey(os.path.join(path, "left.png")), grey(os.path.join(path, "right.png"))
+    H, W = left.shape
+    L = 16
+    D = stereo_costs_u8(left, right, L, 20)
+    V = synth.sm_table(L, synth.TRUNC_LINEAR, 10, 20, dtype=np.int32)
+    lab = oracle.ref_hbp(D, V, synth.TRUNC_LINEAR, 10, 20, 1, 30)
+    gold["cases"]["stereo_png_384x288_L16"] = dict(
+        kind="stereo_png", W=W, H=H, L=L, levels=1, iters=30, cap=20, scale=10, trunc=20, cost_sha=sha(D),
+        table_sha=sha(V), labels_sha=sha(lab), energy_ref_type=float(oracle.ref_energy(D, V, synth.TRUNC_LINEAR,
+                                                                                         10, 20, lab)),
+        source="examples/stereo/left.png, right.png (grey: (299 R + 587 G + 114 B + 500) / 1000)")
+    arrays["stereo_png_384x288_L16/left"] = left
+    arrays["stereo_png_384x288_L16/right"] = right
+    arrays["stereo_png_384x288_L16/labels"] = lab.astype(np.int8)
+    print("stereo PNG case done", flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--skip-large", action="store_true", help="skip the 1920x1080 reference HBP run (minutes)")
+    ap.add_argument("--only-stereo-png", action="store_true",
+                    help="keep every existing fixture and (re)write only the stereo PNG case")
     args = ap.parse_args()
     oracle.build(with_ref=True)
     assert oracle.ref() is not None, "the reference bridge did not build"
+    if args.only_stereo_png:
+        with open(os.path.join(HERE, "golden.json")) as f:
+            gold = json.load(f)
+        arrays = dict(np.load(os.path.join(HERE, "golden_arrays.npz")))
+        stereo_png_case(gold, arrays)
+        write(gold, arrays)
+        return
     gold = {"generator": "tests/golden/make_golden.py", "cases": {}}
     arrays = {}
+    stereo_png_case(gold, arrays)
 
     for (name, W, H, L, seed, model, scale, trunc, dtype, iters) in SMALL_BP:
         P = small_problem(W, H, L, seed, model, scale, trunc, dtype)
@@ -150,6 +186,10 @@ def main():
             reference_seconds_1core=t_ref)
         print("HBP workload done", t_ref, flush=True)
 
+    write(gold, arrays)
+
+
+def write(gold, arrays):
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(gold, f, indent=1, sort_keys=True)
     np.savez_compressed(os.path.join(HERE, "golden_arrays.npz"), **arrays)

@@ -215,6 +215,36 @@ def test_stereo_cost_kernel_bit_exact(ginf):
     assert torch.equal(out, out2)
 
 
+def test_reference_stereo_example_end_to_end(ginf, golden):
+    """The reference example on its own stereo pair (examples/stereo/stereo.cc:
+    16-43): 8-bit grey images -> the integer cost volume on the GPU
+    (ginf_stereo_costs_u8: min(|L(x) - R(x-k)|, 20) for x >= L-1, zero
+    elsewhere) -> Grid<int> loopy BP, TruncLinear(10, 20), 30 iterations.
+    Costs and labels must equal what the reference's own code produced
+    (golden SHA-256), from device and from host images."""
+    import torch
+    meta, arr = golden
+    name = "stereo_png_384x288_L16"
+    case = meta["cases"][name]
+    left, right = arr[name + "/left"], arr[name + "/right"]
+    H, W, L = case["H"], case["W"], case["L"]
+    V = _dev(synth.sm_table(L, synth.TRUNC_LINEAR, case["scale"], case["trunc"], dtype=np.int32))
+    for src in ("device", "host"):
+        D = torch.full((L, H, W), -1, dtype=torch.int32, device="cuda")   # every element must be written
+        if src == "device":
+            ginf.stereo_costs_u8(_dev(left), _dev(right), L, case["cap"], D)
+        else:
+            ginf.stereo_costs_u8(left, right, L, case["cap"], D)
+        assert sha(D.cpu().numpy()) == case["cost_sha"], src
+        lab = torch.zeros((H, W), dtype=torch.int32, device="cuda")
+        ginf.decode_hbp(D, V, synth.TRUNC_LINEAR, 1, case["iters"], labels=lab)
+        got = lab.cpu().numpy()
+        assert sha(got) == case["labels_sha"], src
+        assert np.array_equal(got, arr[name + "/labels"].astype(np.int32)), src
+        e = ginf.energy(D, V, synth.TRUNC_LINEAR, lab)
+        assert e == case["energy_ref_type"], src
+
+
 def test_errors_are_reported_not_fatal(ginf):
     P = synth.random_problem(10, 8, 4, 1)
     with pytest.raises(ginf.GinfError) as e:

@@ -44,65 +44,45 @@ def test_oracle_vs_reference(orc, W, H, L, seed, model):
         np.float32(orc.ref_energy(P.D, P.V, model, P.scale, P.trunc, mine))
 
 
-def test_oracle_stereo_png_vs_reference(orc):
+def test_oracle_stereo_png_vs_reference(orc, golden):
     """Real data: the reference example's stereo pair (stereo.cc:28-45 recipe:
     Grid<int>, L=16, cost min(|L - R(x-k)|, 20) for x >= L-1, TruncLinear(10, 20),
-    30 iterations), decoded by the oracle and by the reference."""
+    30 iterations), decoded by the oracle and by the reference; the grey
+    images and labels stored in the golden fixtures are what they give."""
     _need_ref(orc)
     import os
-    import struct
-    import zlib
+    from golden.png_grey import grey, stereo_costs_u8
     path = os.path.join(orc.REF_SRC, "examples", "stereo")
-
-    def gray(png):
-        data = open(png, "rb").read()
-        w, h, depth, ctype = struct.unpack(">IIBB", data[16:26])
-        chunks, pos = b"", 8
-        while pos < len(data):
-            n = struct.unpack(">I", data[pos:pos + 4])[0]
-            if data[pos + 4:pos + 8] == b"IDAT":
-                chunks += data[pos + 8:pos + 8 + n]
-            pos += 12 + n
-        raw = zlib.decompress(chunks)
-        ch = {0: 1, 2: 3, 6: 4}[ctype]
-        stride = w * ch
-        out = np.zeros((h, stride), np.int64)
-        prev = np.zeros(stride, np.int64)
-        for y in range(h):
-            f = raw[y * (stride + 1)]
-            line = np.frombuffer(raw[y * (stride + 1) + 1:(y + 1) * (stride + 1)], np.uint8).astype(np.int64)
-            cur = np.zeros(stride, np.int64)
-            for x in range(stride):
-                a = cur[x - ch] if x >= ch else 0
-                b = prev[x]
-                c = prev[x - ch] if x >= ch else 0
-                if f == 0: p = 0
-                elif f == 1: p = a
-                elif f == 2: p = b
-                elif f == 3: p = (a + b) // 2
-                else:
-                    pa, pb, pc = abs(b - c), abs(a - c), abs(a + b - 2 * c)
-                    p = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
-                cur[x] = (line[x] + p) & 255
-            out[y] = cur
-            prev = cur
-        px = out.reshape(h, w, ch)
-        if ch == 1:
-            return px[:, :, 0]
-        r, g, b = px[:, :, 0], px[:, :, 1], px[:, :, 2]
-        return (r * 299 + g * 587 + b * 114 + 500) // 1000   # luma; any fixed grey map serves as test data
     if not os.path.exists(os.path.join(path, "left.png")):
         pytest.skip("stereo pair not present")
-    left, right = gray(os.path.join(path, "left.png")), gray(os.path.join(path, "right.png"))
-    H, W = left.shape
+    left, right = grey(os.path.join(path, "left.png")), grey(os.path.join(path, "right.png"))
     L = 16
-    D = np.zeros((L, H, W), np.int32)
-    for k in range(L):
-        D[k, :, L - 1:] = np.minimum(np.abs(left[:, L - 1:] - right[:, L - 1 - k:W - k]), 20)
+    D = stereo_costs_u8(left, right, L, 20)
     V = synth.sm_table(L, synth.TRUNC_LINEAR, 10, 20, dtype=np.int32)
     mine, _ = orc.hbp(D, V, synth.TRUNC_LINEAR, 1, 30)
     ref = orc.ref_hbp(D, V, synth.TRUNC_LINEAR, 10, 20, 1, 30)
     assert np.array_equal(mine, ref)
+    meta, arr = golden
+    case = meta["cases"]["stereo_png_384x288_L16"]
+    assert np.array_equal(arr["stereo_png_384x288_L16/left"], left)
+    assert np.array_equal(arr["stereo_png_384x288_L16/right"], right)
+    assert sha(D) == case["cost_sha"] and sha(ref) == case["labels_sha"]
+
+
+def test_oracle_matches_golden_stereo_png(orc, golden):
+    """The reference example's stereo pair from the stored grey images (no
+    reference checkout needed): the oracle's costs and labels equal the
+    reference's (golden SHA-256)."""
+    from golden.png_grey import stereo_costs_u8
+    meta, arr = golden
+    name = "stereo_png_384x288_L16"
+    case = meta["cases"][name]
+    D = stereo_costs_u8(arr[name + "/left"], arr[name + "/right"], case["L"], case["cap"])
+    assert sha(D) == case["cost_sha"]
+    V = synth.sm_table(case["L"], synth.TRUNC_LINEAR, case["scale"], case["trunc"], dtype=np.int32)
+    lab, _ = orc.hbp(D, V, synth.TRUNC_LINEAR, 1, case["iters"])
+    assert sha(lab) == case["labels_sha"]
+    assert orc.energy(D, V, lab, exact_type=True) == case["energy_ref_type"]
 
 
 def test_oracle_matches_golden_small(orc, golden):
