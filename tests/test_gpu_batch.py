@@ -132,3 +132,43 @@ def test_stream_ordered_replays(ginf):
     finally:
         for pl in plans:
             pl.close()
+
+
+def test_batch_workload_scale_vs_oracle(ginf, orc, tmp_path, monkeypatch):
+    """The seeded 64-grid batch workload (sizes 200x150 .. 1280x720, L in
+    {16, 32, 64}, 30 half-sweeps, costs built on the GPU) plus two grids at
+    the edges of its range -- the full 1280x720 x 64 and a non-exact label
+    count (L = 48) -- solved by one autotuned plan.  Every grid must equal its
+    single-grid solve, and the largest, the smallest, the first grid of each
+    label count and the L = 48 grid must equal the CPU oracle's loopy BP
+    (the reference's decodeBp, src/bp.cc:182-187) bit for bit."""
+    import torch
+    monkeypatch.setenv("GINF_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    iters = 30
+    shapes = synth.batch_shapes(64, seed=2) + [(1280, 720, 64), (1001, 433, 48)]
+    pairs, problems, labels = [], [], []
+    for i, (W, H, L) in enumerate(shapes):
+        pair = synth.stereo_pair(W, H, L, 12, 2.0, seed=100 + i)
+        D = torch.empty((L, H, W), dtype=torch.float32, device="cuda")
+        ginf.stereo_costs(torch.from_numpy(pair.left).cuda(), torch.from_numpy(pair.right).cuda(), L, 0.07, 15.0, D)
+        V = torch.from_numpy(synth.sm_table(L, synth.TRUNC_LINEAR, 1.0, 1.7)).cuda()
+        pairs.append(pair)
+        problems.append((D, V, synth.TRUNC_LINEAR))
+        labels.append(torch.zeros((H, W), dtype=torch.int32, device="cuda"))
+    with ginf.Batch(problems, labels, iters, autotune=0) as b:
+        assert b.config()["tuned_now"] is True
+        b.run()
+        got = [l.cpu().numpy() for l in labels]
+    want = _single(ginf, problems, iters)
+    for g, (a, w) in enumerate(zip(got, want)):
+        assert np.array_equal(a, w), (g, shapes[g])
+    size = [W * H * L for W, H, L in shapes]
+    pick = {int(np.argmax(size)), int(np.argmin(size)), len(shapes) - 1}
+    for L in (16, 32, 64):
+        pick.add(next(i for i, s in enumerate(shapes) if s[2] == L))
+    assert len(shapes) - 2 in pick   # 1280x720x64 is the largest
+    for g in sorted(pick):
+        W, H, L = shapes[g]
+        D = synth.cost_volume(pairs[g], L, 0.07, 15.0)
+        lab, _ = orc.hbp(D, synth.sm_table(L, synth.TRUNC_LINEAR, 1.0, 1.7), synth.TRUNC_LINEAR, 1, iters)
+        assert np.array_equal(got[g], lab), (g, shapes[g])
