@@ -289,7 +289,7 @@ def run_ours(args, cfg):
     lab = torch.zeros((cfg["H"], cfg["W"]), dtype=torch.int32, device=dev)
     ws = capi.Workspace()
     stream = torch.cuda.current_stream(dev)
-    opt = dict(stream=stream.cuda_stream, tile_nodes=args.tile_nodes)
+    opt = dict(stream=stream.cuda_stream, tile_nodes=args.tile_nodes, sweeps_per_launch=args.sweeps_per_launch)
 
     def step():
         return capi.solve(D, V, P.model, cfg["levels"], cfg["iters"], cfg["icm"], labels=lab, workspace=ws,
@@ -806,7 +806,8 @@ def main():
     ap.add_argument("--verbose", action="store_true")
     ap.add_argument("--retune", action="store_true", help="batch workload: re-measure the autotuner's choice")
     ap.add_argument("--sweeps-per-launch", type=int, default=0,
-                    help="batch workload: half-sweeps per persistent launch (0: autotuned, with --tile-nodes 0)")
+                    help="batch workload: half-sweeps per persistent launch (0: autotuned, with --tile-nodes 0); "
+                         "single grids: most half-sweeps per cluster launch (0: default, 1: one per launch)")
     ap.add_argument("--size", default=None, help="WxH override of the workload's grid size (profiling runs)")
     ap.add_argument("--grids", type=int, default=0,
                     help="batch workload: number of grids (profiling runs; default 64)")

@@ -8,6 +8,8 @@
 // drained, with the device status word checked.
 #include <cuda_fp16.h>
 
+#include <algorithm>
+#include <climits>
 #include <cstdio>
 #include <atomic>
 #include <cstring>
@@ -214,6 +216,7 @@ struct Resolved {
     int decode;
     int host_access;
     int async;
+    int cluster_k;  // most half-sweeps per temporal-blocking launch; 0 = one per launch
     SweepConfig cfg;
     cudaStream_t stream;
 };
@@ -249,6 +252,8 @@ ginf_status resolve(const ginf_grid *g, const ginf_options *o, Resolved &r) {
     if (o->host_access != GINF_HOST_AUTO && o->host_access != GINF_HOST_COPY)
         return fail(GINF_ERR_INVALID_ARGUMENT, "unknown host_access");
     r.host_access = o->host_access;
+    if (o->sweeps_per_launch < 0) return fail(GINF_ERR_INVALID_ARGUMENT, "sweeps_per_launch must be >= 0");
+    r.cluster_k = o->sweeps_per_launch >= 2 ? o->sweeps_per_launch : 0;
     r.async = o->stream_ordered != 0;
     r.stream = static_cast<cudaStream_t>(o->stream);
     return GINF_OK;
@@ -300,6 +305,7 @@ struct Prepared {
     RecordFormat f;
     std::vector<Level> lv;
     unsigned char *rec = nullptr;  // records of all levels
+    unsigned char *rec2 = nullptr; // second record buffer of the temporal-blocking launches (largest level)
     void *Vt = nullptr;            // table in the compute type
     int32_t *lab = nullptr;        // device labels (caller's or a copy)
     int32_t *lab2 = nullptr;       // second label buffer (ICM ping-pong)
@@ -347,8 +353,12 @@ ginf_status prepare(Call &c, Prepared &P, int levels, bool want_lab2, const int3
     // Host costs the device can read in place are read by the layout
     // transform itself (the transfer fused into it); others are staged.
     const void *host_view = host && c.r.host_access == GINF_HOST_AUTO ? host_device_view(g->data_costs) : nullptr;
+    // Temporal blocking alternates between a level's records and a second
+    // buffer as large as the largest level.
+    const bool two_buffers = bp && c.r.cluster_k >= 2 && cluster_sweep_eligible(P.f, c.r.mode);
     Arena a;
     const size_t id_rec = a.add(rec_total);
+    const size_t id_rec2 = two_buffers ? a.add((size_t)W * H * P.f.rec_bytes) : 0;
     const size_t id_stage = host && !host_view ? a.add(cost_bytes) : 0;
     const size_t id_tin = a.add(table_in);
     const size_t id_t = a.add(table_t);
@@ -359,6 +369,7 @@ ginf_status prepare(Call &c, Prepared &P, int levels, bool want_lab2, const int3
     GINF_TRY(ws_reserve(c.ws, a.total()));
     unsigned char *base = c.ws->arena;
     P.rec = a.ptr(base, id_rec);
+    P.rec2 = two_buffers ? a.ptr(base, id_rec2) : nullptr;
     P.Vt = a.ptr(base, id_t);
     P.lab = labels_dev ? labels_dev : reinterpret_cast<int32_t *>(a.ptr(base, id_lab));
     P.lab2 = want_lab2 ? reinterpret_cast<int32_t *>(a.ptr(base, id_lab2)) : nullptr;
@@ -522,7 +533,23 @@ ginf_status run_levels(Call &c, Prepared &P, int iters, int64_t &nli, int from, 
         p.tiles_per_row = (n1 + c.r.cfg.nt - 1) / c.r.cfg.nt;
         p.num_tiles = (lv.H - 2) * p.tiles_per_row;
         p.status = P.status;
-        for (int it = 0; it < iters; ++it) {
+        // Half-sweeps [0, it_end) run one per launch; the rest, when the level
+        // qualifies, several per launch in an even number of temporal-blocking
+        // launches that alternate between the records and the second buffer
+        // (so the level ends in its own records).  A level fed from the
+        // coarser one takes its first half-sweep one per launch.
+        int it_end = iters;
+        int nlaunch = 0, kmax = 0;
+        if (P.rec2 && iters >= 2) {
+            const int start = first == RD_COARSE ? 1 : 0;
+            const int rem = iters - start;
+            kmax = std::min(c.r.cluster_k, cluster_sweep_max_halo(f.L));
+            nlaunch = (rem + kmax - 1) / kmax;
+            if (nlaunch % 2) ++nlaunch;
+            if (rem >= 2 && nlaunch <= rem) it_end = start;
+            else nlaunch = 0;
+        }
+        for (int it = 0; it < it_end; ++it) {
             p.iter = it;
             p.read_mode = it == 0 ? first : RD_OWN;
             p.write_labels = (t == 0 && stale && it >= iters - 2) ? 1 : 0;
@@ -531,6 +558,39 @@ ginf_status run_levels(Call &c, Prepared &P, int iters, int64_t &nli, int from, 
             if (t == 0 && c.stats) {
                 ++c.stats->level0_sweep_launches;
                 c.stats->level0_alg_bytes += sweep_alg_bytes(f, lv);
+            }
+        }
+        if (nlaunch > 0) {
+            ClusterSweepParams q{};
+            q.W = lv.W;
+            q.H = lv.H;
+            q.L = f.L;
+            q.rec_bytes = f.rec_bytes;
+            q.d_bytes = f.d_bytes;
+            q.m_bytes = f.m_bytes;
+            q.slot_bytes = f.slot_bytes;
+            q.from_stride = cluster_from_stride(f);
+            q.norm_min = c.r.norm_min;
+            q.V = P.Vt;
+            q.labels = P.lab;
+            q.status = P.status;
+            q.label_from = (t == 0 && stale) ? iters - 2 : INT_MAX;
+            const int rem = iters - it_end;
+            int it0 = it_end;
+            for (int l = 0; l < nlaunch; ++l) {
+                q.k = rem / nlaunch + (l < rem % nlaunch ? 1 : 0);
+                q.iter0 = it0;
+                q.rec_in = l % 2 == 0 ? rec : P.rec2;
+                q.rec_out = l % 2 == 0 ? P.rec2 : rec;
+                q.write_d = l == 0 ? 1 : 0;
+                q.read_mode = (l == 0 && it_end == 0 && first == RD_ZERO) ? RD_ZERO : RD_OWN;
+                GINF_CK(launch_cluster_sweeps(f, q, s));
+                ++c.launches;
+                if (t == 0 && c.stats) {
+                    ++c.stats->level0_sweep_launches;
+                    c.stats->level0_alg_bytes += q.k * sweep_alg_bytes(f, lv);
+                }
+                it0 += q.k;
             }
         }
         nli += (int64_t)lv.W * lv.H * f.L * iters;

@@ -68,6 +68,39 @@ struct SweepParams {
     int *status;
 };
 
+// Parameters of one launch of the temporal-blocking kernel (several
+// half-sweeps of one level, FP32 records, L <= 32; sweep_cluster.cu).
+struct ClusterSweepParams {
+    int W, H, L;
+    uint32_t rec_bytes, d_bytes, m_bytes, slot_bytes;
+    uint32_t from_stride;          // bytes per belief vector in shared memory (odd number of 16-byte chunks)
+    const unsigned char *rec_in;   // records read (this level, one buffer) ...
+    unsigned char *rec_out;        // ... and written (the other buffer)
+    int iter0;                     // level half-sweep index of the launch's first half-sweep
+    int k;                         // half-sweeps in this launch (also the halo depth)
+    int label_from;                // half-sweeps with index >= label_from write labels (INT_MAX: none)
+    int read_mode;                 // RD_OWN, or RD_ZERO (messages start at zero)
+    int write_d;                   // 1: write whole records (rec_out lacks the costs), 0: messages only
+    int norm_min;
+    const void *V;
+    int32_t *labels;
+    int *status;
+    int bw, bh;                    // sub-block of one CTA (set by the launcher)
+};
+
+// Launches of the temporal-blocking kernel; eligible formats: FP32
+// arithmetic, native store, L <= 32.
+cudaError_t launch_cluster_sweeps(const RecordFormat &f, const ClusterSweepParams &p, cudaStream_t s);
+// Deepest halo (most half-sweeps per launch) the kernel's region allows.
+int cluster_sweep_max_halo(int L);
+inline bool cluster_sweep_eligible(const RecordFormat &f, int mode) {
+    return f.ctype == CT_F32 && f.store == ST_NATIVE && mode == MODE_LINEAR && f.L <= 32;
+}
+inline uint32_t cluster_from_stride(const RecordFormat &f) {
+    const uint32_t chunks = f.d_bytes / 16;
+    return 16u * (chunks % 2 == 0 ? chunks + 1 : chunks);
+}
+
 // Per-kernel launch state kept across calls, safe for concurrent host
 // threads and separate per device (kernel attributes and occupancy belong to
 // a device).  Instances live in static storage, where the atomics start at 0.

@@ -120,6 +120,61 @@ __device__ __forceinline__ void fence_proxy_async_global() {
 __device__ __forceinline__ void launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
+// Thread-block clusters: this CTA's coordinates inside its cluster, the
+// cluster's shape, and the cluster's coordinates in the grid of clusters.
+__device__ __forceinline__ uint32_t cluster_ctaid_x() {
+    uint32_t v;
+    asm("mov.u32 %0, %%cluster_ctaid.x;" : "=r"(v));
+    return v;
+}
+__device__ __forceinline__ uint32_t cluster_ctaid_y() {
+    uint32_t v;
+    asm("mov.u32 %0, %%cluster_ctaid.y;" : "=r"(v));
+    return v;
+}
+__device__ __forceinline__ uint32_t cluster_nctaid_x() {
+    uint32_t v;
+    asm("mov.u32 %0, %%cluster_nctaid.x;" : "=r"(v));
+    return v;
+}
+__device__ __forceinline__ uint32_t cluster_nctaid_y() {
+    uint32_t v;
+    asm("mov.u32 %0, %%cluster_nctaid.y;" : "=r"(v));
+    return v;
+}
+__device__ __forceinline__ uint32_t clusterid_x() {
+    uint32_t v;
+    asm("mov.u32 %0, %%clusterid.x;" : "=r"(v));
+    return v;
+}
+__device__ __forceinline__ uint32_t clusterid_y() {
+    uint32_t v;
+    asm("mov.u32 %0, %%clusterid.y;" : "=r"(v));
+    return v;
+}
+
+// The distributed-shared-memory address of the same offset in the shared
+// memory of CTA `rank` of this cluster.
+__device__ __forceinline__ uint32_t dsmem_addr(uint32_t local_smem_addr, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local_smem_addr), "r"(rank));
+    return r;
+}
+
+// 16-byte store into (possibly another CTA's) shared memory of this cluster.
+__device__ __forceinline__ void st_dsmem_v4(uint32_t addr, float a, float b, float c, float d) {
+    asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(a), "f"(b), "f"(c), "f"(d)
+                 : "memory");
+}
+
+// Cluster-wide barrier: every thread of every CTA of the cluster arrives
+// (release: its earlier shared-memory writes, local and remote, become
+// visible) and waits (acquire).  Must be reached by all threads, convergently.
+__device__ __forceinline__ void cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 // Grid-wide barrier for a cooperative launch (all blocks co-resident).  bar
 // holds {arrived, generation}, zeroed before the launch.  The last block to
 // arrive resets the count and advances the generation; the others wait for

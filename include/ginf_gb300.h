@@ -82,7 +82,15 @@ typedef struct ginf_options {
     int32_t tile_nodes;      /* nodes per sweep tile (8, 16 or 32); 0 = default
                                 (16), or the autotuned choice for batches        */
     int32_t sweeps_per_launch; /* batches: half-sweeps per persistent launch;
-                                  0 = autotuned                                */
+                                  0 = autotuned.  Single grids: 0 or 1 = one
+                                  half-sweep per launch (default); k >= 2 =
+                                  temporal blocking on FP32 grids with
+                                  L <= 32 and the Potts / truncated-linear
+                                  update: up to k half-sweeps per launch on
+                                  thread-block clusters, the same results bit
+                                  for bit (slower than one per launch on
+                                  GB300 at these label counts, where the
+                                  update is latency-bound, not HBM-bound)   */
     int32_t autotune;        /* batches: 0 = cached choice, else measure and cache;
                                 1 = always measure; -1 = never (defaults)        */
     void *stream;            /* cudaStream_t to run on; NULL = legacy default */

@@ -460,3 +460,35 @@ def test_bounded_waits_time_out_and_the_device_stays_usable(ginf, orc):
     want, _ = orc.hbp(P.D, P.V, P.model, 2, 4)
     got = ginf.decode_hbp(P.D, P.V, P.model, 2, 4)
     assert np.array_equal(got[1:-1, 1:-1], want[1:-1, 1:-1])
+
+
+@pytest.mark.parametrize("W,H,L,levels,iters", [(384, 288, 16, 1, 50), (203, 157, 32, 1, 13), (97, 71, 5, 1, 9),
+                                                (130, 91, 24, 1, 7), (61, 250, 12, 2, 6), (300, 41, 31, 3, 5),
+                                                (3, 3, 16, 1, 4), (4, 50, 16, 1, 3), (200, 3, 32, 1, 2),
+                                                (1025, 257, 16, 1, 20), (515, 300, 32, 4, 10)])
+def test_cluster_temporal_blocking_bit_exact(ginf, orc, W, H, L, levels, iters):
+    """Several half-sweeps per launch on thread-block clusters (FP32, L <= 32):
+    labels and messages equal the one-half-sweep-per-launch kernel for every
+    halo depth tried, and the oracle."""
+    P = synth.random_problem(W, H, L, 7 * W + H, model=synth.TRUNC_LINEAR if L % 2 else synth.POTTS,
+                             scale=1.0 if L % 2 else 0.6, trunc=2.2)
+    D, V = _dev(P.D), _dev(P.V)
+    lab1, msg1 = ginf.decode_hbp(D, V, P.model, levels, iters, want_msgs=True)
+    for k in (2, 3, 5, 8, 15):
+        lab, msg = ginf.decode_hbp(D, V, P.model, levels, iters, want_msgs=True, sweeps_per_launch=k)
+        assert np.array_equal(lab.cpu().numpy(), lab1.cpu().numpy()), k
+        assert np.array_equal(msg.cpu().numpy().view(np.uint32), msg1.cpu().numpy().view(np.uint32)), k
+    if W * H * L * iters <= 4e7:
+        want, _ = orc.hbp(P.D, P.V, P.model, levels, iters)
+        assert np.array_equal(lab1.cpu().numpy(), want)
+
+
+def test_cluster_launch_schedule(ginf):
+    """sweeps_per_launch = 8 runs the 384x288x16 workload's 50 half-sweeps in
+    an even number of cluster launches (8), so the level ends in its own
+    records; the default runs one half-sweep per launch."""
+    P = synth.workload_plain_bp()
+    _, st = ginf.decode_hbp(_dev(P.D), _dev(P.V), P.model, 1, 50, want_stats=True, sweeps_per_launch=8)
+    assert st["level0_sweep_launches"] == 8
+    _, st1 = ginf.decode_hbp(_dev(P.D), _dev(P.V), P.model, 1, 50, want_stats=True)
+    assert st1["level0_sweep_launches"] == 50
