@@ -447,7 +447,18 @@ int quad_radius_host(const std::vector<unsigned char> &col, int L) {
     return r;
 }
 
-ginf_status table_radius(Call &c, Prepared &P, int &radius) {
+// Whether V(0,0) = 0 and V(0,k) = V(0,1) k^2 exactly for k <= r (the pass
+// form of the quadratic transform assumes that profile).
+template <typename T>
+bool quad_exact_host(const std::vector<unsigned char> &col, int r) {
+    const T *v = reinterpret_cast<const T *>(col.data());
+    if (!(v[0] == T(0))) return false;
+    for (int k = 1; k <= r; ++k)
+        if (!(v[k] == v[1] * T(k * k))) return false;
+    return true;
+}
+
+ginf_status table_radius(Call &c, Prepared &P, int &radius, int &exact) {
     const int L = P.f.L;
     std::vector<unsigned char> col((size_t)L * P.f.t_size);
     // V(0,k) = V[L*k]: one element per table row.
@@ -455,6 +466,8 @@ ginf_status table_radius(Call &c, Prepared &P, int &radius) {
                               cudaMemcpyDeviceToHost, c.r.stream));
     GINF_CK(cudaStreamSynchronize(c.r.stream));
     radius = P.f.ctype == CT_F64 ? quad_radius_host<double>(col, L) : quad_radius_host<float>(col, L);
+    exact = 0;
+    if (P.f.ctype == CT_F32 && radius <= 4) exact = quad_exact_host<float>(col, radius) ? 1 : 0;
     return GINF_OK;
 }
 
@@ -472,8 +485,8 @@ int64_t sweep_alg_bytes(const RecordFormat &f, const Level &lv) {
 ginf_status run_levels(Call &c, Prepared &P, int iters, int64_t &nli, int from, int to, bool top_initialised) {
     const RecordFormat &f = P.f;
     cudaStream_t s = c.r.stream;
-    int radius = 9;
-    if (c.r.mode == MODE_STD_QUAD) GINF_TRY(table_radius(c, P, radius));
+    int radius = 9, quad_exact = 0;
+    if (c.r.mode == MODE_STD_QUAD) GINF_TRY(table_radius(c, P, radius, quad_exact));
     const int T = (int)P.lv.size();
     const bool stale = c.r.decode == GINF_DECODE_STALE;
     const int W0 = P.lv[0].W, H0 = P.lv[0].H;
@@ -530,6 +543,7 @@ ginf_status run_levels(Call &c, Prepared &P, int iters, int64_t &nli, int from, 
         p.V = P.Vt;
         p.labels = P.lab;
         p.quad_radius = radius;
+        p.quad_exact = quad_exact;
         p.tiles_per_row = (n1 + c.r.cfg.nt - 1) / c.r.cfg.nt;
         p.num_tiles = (lv.H - 2) * p.tiles_per_row;
         p.status = P.status;

@@ -65,6 +65,7 @@ struct SweepParams {
     int write_labels;
     int tiles_per_row, num_tiles;  // set by the launcher for the variant it runs
     int quad_radius;               // truncation radius of a quadratic table (kernel choice only)
+    int quad_exact;                // 1: V(0,k) = V(0,1) k^2 exactly up to that radius, V(0,0) = 0
     int *status;
 };
 

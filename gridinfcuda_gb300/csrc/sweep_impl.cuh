@@ -602,7 +602,84 @@ __device__ void message_std_quad(const SweepParams &p, unsigned char *slot, int 
     }
 }
 
-enum { KIND_LINEAR = 0, KIND_QUAD = 1, KIND_GENERAL = 2, KIND_QUAD4 = 3 };
+// FP16 message store, truncated quadratic table V(0,k) = s k^2 (k <= r <= 4),
+// min-normalised: the distance transform as r passes
+//   m_j(i) = min(m_{j-1}(i), m_{j-1}(i-1) + s (2j-1), m_{j-1}(i+1) + s (2j-1))
+// from m_0 = h.  A path of j steps that moves at k of them pays at least
+// s (1 + 3 + ... + (2k-1)) = s k^2, the first k steps, so in exact arithmetic
+// m_r(i) = min_{|k| <= r} h(i+k) + s k^2: the window's value, with the sums
+// rounded step by step instead of once (this store is judged against the
+// FP64 run within a tolerance, not bit for bit).  Per output and pass one
+// packed addition for two outputs and one three-input minimum, against the
+// window's four pair minima, two three-input minima and the additions.  The
+// minimum output stays min(h) exactly (every candidate beside h(i) adds a
+// positive increment), so the min-normalised message is 0 at its argmin.
+// Passes beyond r get an infinite increment and change nothing.
+constexpr int kQuadPasses = 4;
+template <typename M, int LMAX, bool EXACT>
+__device__ __forceinline__ void message_quad_passes(const SweepParams &p, unsigned char *slot, int L, int dir,
+                                                    const float *cpass, float trunc) {
+    constexpr int B = MIO<M, float>::B;
+    static_assert(LMAX % 2 == 0, "outputs come in pairs");
+    const float inf = pos_inf<float>();
+    unsigned char *md = slot + p.d_bytes + dir * p.m_bytes;
+    float m[LMAX];
+#pragma unroll
+    for (int c = 0; c < LMAX; c += B) {
+        if (EXACT || c < L) {
+            float a[B], f[B];
+            MIO<M, float>::load(md + c * sizeof(M), a);
+            load_t<float, B>(slot + c * sizeof(float), f);
+#pragma unroll
+            for (int k = 0; k < B; k += 2) {
+                const float2 d = sub_f32x2(f[k], f[k + 1], a[k], a[k + 1]);
+                m[c + k] = (EXACT || c + k < L) ? d.x : inf;
+                m[c + k + 1] = (EXACT || c + k + 1 < L) ? d.y : inf;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < B; ++k) m[c + k] = inf;
+        }
+    }
+    // min(h), three values at a time (labels beyond L hold +inf).
+    float minh = fminf(m[0], m[1]);
+#pragma unroll
+    for (int i = 2; i < LMAX; i += 2) minh = min3_f32(minh, m[i], m[i + 1]);
+    const float cap = minh + trunc;
+#pragma unroll
+    for (int j = 0; j < kQuadPasses; ++j) {
+        const float c = cpass[j];
+        // p(i) = m(i) + c of the previous pass, two outputs per addition:
+        // pprev = (p(i-2), p(i-1)), pcur = (p(i), p(i+1)), pnext = (p(i+2), p(i+3)).
+        float2 pprev = make_float2(inf, inf);
+        float2 pcur = add_f32x2(m[0], m[1], c, c);
+#pragma unroll
+        for (int i = 0; i < LMAX; i += 2) {
+            const float2 pnext = i + 2 < LMAX ? add_f32x2(m[i + 2], m[i + 3], c, c) : make_float2(inf, inf);
+            const float n0 = min3_f32(m[i], pprev.y, pcur.y);
+            const float n1 = min3_f32(m[i + 1], pcur.x, pnext.x);
+            m[i] = n0;
+            m[i + 1] = n1;
+            pprev = pcur;
+            pcur = pnext;
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < LMAX; c += B) {
+        if (EXACT || c < L) {
+            float r[B];
+#pragma unroll
+            for (int k = 0; k < B; k += 2) {
+                const float2 o = sub_f32x2(fminf(m[c + k], cap), fminf(m[c + k + 1], cap), minh, minh);
+                r[k] = o.x;
+                r[k + 1] = o.y;
+            }
+            MIO<M, float>::store(md + c * sizeof(M), r);
+        }
+    }
+}
+
+enum { KIND_LINEAR = 0, KIND_QUAD = 1, KIND_GENERAL = 2, KIND_QUAD4 = 3, KIND_QUADPASS = 4 };
 
 // Constants a launch reads from its smoothness table: slope V(0,1) and
 // truncation V(0,L-1) (bp.cc:35,43), and for the quadratic kernels the taps
@@ -611,6 +688,7 @@ template <typename T>
 struct TableConsts {
     T scale, trunc;
     T vtap[kQuadWindow + 1];
+    T cpass[kQuadPasses];  // KIND_QUADPASS: increments s (2j-1), +inf beyond the radius
     int qr;
 };
 
@@ -625,6 +703,11 @@ __device__ __forceinline__ TableConsts<T> table_consts(const void *V, int L) {
         tc.qr = quad_radius(Vt, L, tc.trunc);
 #pragma unroll
         for (int k = 0; k <= kQuadWindow; ++k) tc.vtap[k] = k <= tc.qr ? __ldg(&Vt[(size_t)L * k]) : pos_inf<T>();
+    }
+    if constexpr (KIND == KIND_QUADPASS && sizeof(T) == 4) {
+        tc.qr = quad_radius(Vt, L, tc.trunc);
+#pragma unroll
+        for (int j = 0; j < kQuadPasses; ++j) tc.cpass[j] = j < tc.qr ? tc.scale * T(2 * j + 1) : pos_inf<T>();
     }
     return tc;
 }
@@ -743,6 +826,9 @@ __device__ __forceinline__ bool tile_finish(const SweepParams &p, const TableCon
     if (act) {
         if constexpr (KIND == KIND_LINEAR) {
             message_linear<T, M, LMAX, EXACT>(p, slot, L, dir, tc.scale, tc.trunc);
+        } else if constexpr (KIND == KIND_QUADPASS) {
+            if constexpr (std::is_same<T, float>::value && sizeof(M) == 2)
+                message_quad_passes<M, LMAX, EXACT>(p, slot, L, dir, tc.cpass, tc.trunc);
         } else if constexpr (KIND == KIND_QUAD || KIND == KIND_QUAD4) {
             constexpr int QW = KIND == KIND_QUAD4 ? kQuadWindowSmall : kQuadWindow;
             if constexpr (sizeof(T) == 4 && !std::is_same<T, int>::value) {
@@ -1079,7 +1165,8 @@ cudaError_t launch_tiles(K kern, LaunchCache &lc_state, int NW, int nodes, const
 template <typename T, typename M, int LMAX, bool EXACT, int NW, int KIND, bool DIRECT = false>
 cudaError_t launch_one(const SweepParams &params, uint32_t slot_bytes, cudaStream_t s, int num_sms) {
     static LaunchCache cache;
-    if constexpr ((KIND == KIND_QUAD || KIND == KIND_QUAD4) && sizeof(M) == 2 && LMAX == 128 && !DIRECT) {
+    if constexpr ((KIND == KIND_QUAD || KIND == KIND_QUAD4 || KIND == KIND_QUADPASS) && sizeof(M) == 2 &&
+                  LMAX == 128 && !DIRECT) {
         return launch_tiles(sweep_kernel_bounded<T, M, LMAX, EXACT, NW, KIND, 6>, cache, NW, NW * 8, params,
                             slot_bytes, s, num_sms);
     } else {
@@ -1105,6 +1192,13 @@ cudaError_t launch_variant(const RecordFormat &f, const SweepConfig &cfg, const 
             // FP32 records at L = 128: two warps per eight nodes (register relief).
             if (exact && p.quad_radius <= kQuadWindowSmall) return launch_split<4, 4>(p, f.slot_bytes, s, num_sms);
             if (exact && p.quad_radius <= kQuadWindow) return launch_split<4, 8>(p, f.slot_bytes, s, num_sms);
+        }
+        if constexpr (std::is_same<T, float>::value && sizeof(M) == 2) {
+            // FP16 store and an exactly quadratic table: the pass form.
+            if (p.quad_exact && p.quad_radius <= kQuadPasses) {
+                if (exact) return launch_one<T, M, LM, true, 2, KIND_QUADPASS>(p, f.slot_bytes, s, num_sms);
+                return launch_one<T, M, LM, false, 2, KIND_QUADPASS>(p, f.slot_bytes, s, num_sms);
+            }
         }
         if (p.quad_radius <= kQuadWindowSmall) {
             if (exact) return launch_one<T, M, LM, true, 2, KIND_QUAD4>(p, f.slot_bytes, s, num_sms);

@@ -272,7 +272,10 @@ def test_windowed_quadratic_equals_min_convolution(ginf):
     FP32 records at L = 128 run the split kernel (two warps per eight nodes):
     radius 4 (trunc 25) and radius 7 (trunc 50) windows, the mean and the
     minimum subtracted, FP32 and FP16 messages, 37- and 70-wide grids
-    (partial last tiles), two levels (the coarse-to-fine first sweep)."""
+    (partial last tiles), two levels (the coarse-to-fine first sweep).  FP16
+    cases use a table offset by V(0,0) = 0.5, which keeps them on the window
+    form (an exactly quadratic table with the FP16 store runs the pass form,
+    test_fp16_quadratic_pass_form_vs_min_convolution)."""
     F32, F16 = ginf.STORE_NATIVE, ginf.STORE_F16
     cases = [(128, 25.0, 37, 23, ginf.NORM_MEAN, F32), (128, 25.0, 37, 23, ginf.NORM_MIN, F32),
              (128, 50.0, 70, 41, ginf.NORM_MEAN, F32), (128, 50.0, 70, 41, ginf.NORM_MIN, F32),
@@ -281,12 +284,36 @@ def test_windowed_quadratic_equals_min_convolution(ginf):
              (64, 25.0, 37, 23, ginf.NORM_MIN, F16)]
     for L, trunc, W, H, norm, store in cases:
         P = synth.random_problem(W, H, L, 40 + L, model=synth.TRUNC_QUAD, scale=1.0, trunc=trunc, cost_max=30.0)
+        V = P.V + np.float32(0.5) if store == F16 else P.V
         opt = dict(want_msgs=True, rule=ginf.RULE_STANDARD, normalize=norm, store=store)
-        lq, mq = ginf.decode_hbp(P.D, P.V, synth.TRUNC_QUAD, 2, 5, **opt)
-        lb, mb = ginf.decode_hbp(P.D, P.V, synth.EXPLICIT, 2, 5, **opt)
+        lq, mq = ginf.decode_hbp(P.D, V, synth.TRUNC_QUAD, 2, 5, **opt)
+        lb, mb = ginf.decode_hbp(P.D, V, synth.EXPLICIT, 2, 5, **opt)
         case = (L, trunc, norm, store)
         assert np.array_equal(lq, lb), case
         assert mq.dtype == mb.dtype and np.array_equal(mq.view(np.uint8), mb.view(np.uint8)), case
+
+
+def test_fp16_quadratic_pass_form_vs_min_convolution(ginf):
+    """FP16 store with an exactly quadratic table V(0,k) = s k^2 (radius <= 4):
+    the distance transform runs as r min-plus passes, whose sums round step by
+    step, so it is held to the FP16 store's resolution against the O(L^2)
+    min-convolution: messages within 2^-8 of their largest magnitude (four
+    FP16 steps at the top of the range) after five half-sweeps on two levels,
+    labels equal on >= 99.5 % of the interior, and each message's minimum
+    exactly 0 (min-normalised)."""
+    for L, trunc, W, H, scale in [(128, 25.0, 37, 23, 1.0), (64, 25.0, 37, 23, 1.0), (128, 9.0, 70, 41, 0.6),
+                                  (48, 16.0, 41, 30, 1.0)]:
+        P = synth.random_problem(W, H, L, 60 + L, model=synth.TRUNC_QUAD, scale=scale, trunc=trunc, cost_max=30.0)
+        opt = dict(want_msgs=True, rule=ginf.RULE_STANDARD, normalize=ginf.NORM_MIN, store=ginf.STORE_F16)
+        lq, mq = ginf.decode_hbp(P.D, P.V, synth.TRUNC_QUAD, 2, 5, **opt)
+        lb, mb = ginf.decode_hbp(P.D, P.V, synth.EXPLICIT, 2, 5, **opt)
+        a, b = mq.astype(np.float64), mb.astype(np.float64)
+        case = (L, trunc, scale)
+        assert np.abs(a - b).max() <= 2.0 ** -8 * np.abs(b).max(), case
+        assert (lq[1:-1, 1:-1] == lb[1:-1, 1:-1]).mean() >= 0.995, case
+        inner = a[1:-1, 1:-1]
+        live = np.abs(inner).max(axis=-1) > 0   # slots from interior senders
+        assert (inner.min(axis=-1)[live] == 0).all(), case
 
 
 def test_wide_quadratic_lower_envelope_vs_fp64(ginf, orc):

@@ -215,3 +215,25 @@ def test_bad_seed_falls_back_to_plain_hbp(ginf):
     want = ginf.decode_hbp(P.D, P.V, P.model, 5, 2)
     assert st["warm_start_used"] == 0
     assert np.array_equal(lab.cpu().numpy()[1:-1, 1:-1], want[1:-1, 1:-1])
+
+
+def test_trained_network_beats_the_network_free_guess(ginf):
+    """What the trained network gains over the method without it.  Trained
+    with this library's kernels on BP's own converged messages of 48 seeded
+    256x192x64 planar-stereo grids (40 epochs), it predicts the converged
+    level-1 beliefs (costs plus the finest level's converged incoming
+    messages, block-averaged) of 4 held-out grids with a mean squared error
+    below 0.93 of the network-free guess (the costs alone, y = x); measured
+    0.855.  (Fewer level-0 half-sweeps do not follow: on 1920x1080 grids the
+    prescribed network's seeds still need 7-10 half-sweeps per level against
+    8 for the cold start, because its errors are whole coherent regions.)"""
+    from gridinfcuda_gb300 import warmstart as W
+    X, Y = W.make_training_set(n=48, W=256, H=192, seed0=700000, processes=1, target_iters=30)
+    Xh, Yh = W.make_training_set(n=4, W=256, H=192, seed0=800000, processes=1, target_iters=30)
+    with ginf.WarmNet(64, 32, seed=2) as net:
+        hist = W.train(net, X, Y, epochs=40, batch=8, lr=1e-3)
+        pred = net.forward(Xh)
+    base = float(((Xh - Yh) ** 2).mean())
+    got = float(((pred - Yh) ** 2).mean())
+    assert hist[-1] < hist[0]
+    assert got < 0.93 * base, (got, base)
