@@ -82,6 +82,8 @@ def lib():
                                       ctypes.POINTER(Stats)]
         L.ginf_energy.argtypes = [_p, ctypes.POINTER(Grid), _p, ctypes.POINTER(ctypes.c_double),
                                   ctypes.POINTER(Options)]
+        L.ginf_decode_alpha_beta.argtypes = [_p, ctypes.POINTER(Grid), _p, _i32, _p, ctypes.POINTER(Options),
+                                             ctypes.POINTER(Stats)]
         L.ginf_solve.argtypes = [_p, ctypes.POINTER(Grid), _i32, _i32, _i32, _p, ctypes.POINTER(ctypes.c_double),
                                  ctypes.POINTER(Options), ctypes.POINTER(Stats)]
         L.ginf_stereo_costs.argtypes = [_i32, _i32, _i32, _i32, _p, _p, ctypes.c_float, ctypes.c_float, _p, _p]
@@ -113,7 +115,8 @@ def lib():
                                               ctypes.POINTER(Options), ctypes.POINTER(Stats)]
         L.ginf_decode_hbp_warm.argtypes = [_p, ctypes.POINTER(Grid), _i32, _i32, _i32, _i32, _i32, _p, _i32, _p,
                                            ctypes.POINTER(Options), ctypes.POINTER(Stats)]
-        for name in ("ginf_decode_hbp", "ginf_decode_icm", "ginf_energy", "ginf_solve", "ginf_stereo_costs",
+        for name in ("ginf_decode_hbp", "ginf_decode_icm", "ginf_energy", "ginf_decode_alpha_beta",
+                     "ginf_solve", "ginf_stereo_costs",
                      "ginf_stereo_costs_u8",
                      "ginf_workspace_create", "ginf_workspace_destroy", "ginf_batch_create", "ginf_batch_run",
                      "ginf_batch_config", "ginf_batch_destroy", "ginf_decode_bp_batch", "ginf_warmnet_create",
@@ -259,6 +262,22 @@ def decode_icm(D, V, model, initial, iters, asynchronous=False, *, workspace=Non
     check(lib().ginf_decode_icm(ws, ctypes.byref(g), _ptr(initial)[0], iters, int(asynchronous), _ptr(res)[0],
                                 ctypes.byref(o), ctypes.byref(st) if want_stats else None))
     return (res, st.as_dict()) if want_stats else res
+
+
+def decode_alpha_beta(D, V, model, initial, iters, *, workspace=None, want_stats=False, **opt):
+    """Alpha-beta swap (int32 grids); returns the labelling [, stats]."""
+    L, H, W = D.shape
+    g = make_grid(D, V, model)
+    out = _new_like(D, (H, W), np.int32)
+    init = initial if _ptr(initial)[1] == _ptr(D)[1] else None
+    if init is None:
+        raise ValueError("initial must live in the same memory kind as D")
+    o = options(**opt)
+    st = Stats()
+    ws = workspace.handle if workspace is not None else None
+    check(lib().ginf_decode_alpha_beta(ws, ctypes.byref(g), _ptr(init)[0], iters, _ptr(out)[0], ctypes.byref(o),
+                                       ctypes.byref(st) if want_stats else None))
+    return (out, st.as_dict()) if want_stats else out
 
 
 def energy(D, V, model, labels, *, workspace=None):

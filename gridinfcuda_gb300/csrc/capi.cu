@@ -905,6 +905,87 @@ ginf_status ginf_decode_icm(ginf_workspace *wsp, const ginf_grid *grid, const in
     return finish(c, 0);
 }
 
+ginf_status ginf_decode_alpha_beta(ginf_workspace *wsp, const ginf_grid *grid, const int32_t *initial, int32_t iters,
+                                   int32_t *result, const ginf_options *opt, ginf_stats *stats) {
+    g_last_error.clear();
+    GINF_TRY(check_grid(grid));
+    if (!initial || !result) return fail(GINF_ERR_INVALID_ARGUMENT, "initial / result is NULL");
+    if (iters < 0) return fail(GINF_ERR_INVALID_ARGUMENT, "iters must be >= 0");
+    if (grid->cost_type != GINF_I32)
+        return fail(GINF_ERR_UNSUPPORTED,
+                    "the alpha-beta swap takes int32 grids (the reference instantiates it for int only)");
+    const int W = grid->width, H = grid->height, L = grid->num_labels;
+    const size_t N = (size_t)W * H;
+    if (N > (size_t)0x7ffffff0) return fail(GINF_ERR_INVALID_ARGUMENT, "grid too large for int32 heights");
+    Call c;
+    GINF_TRY(resolve(grid, opt, c.r));
+    WsGuard guard(wsp);
+    c.ws = guard.ws;
+    c.g = grid;
+    c.stats = stats;
+    GINF_TRY(ws_init(c.ws, c.r.stream));
+    begin(c);
+    const bool host = grid->memory == GINF_HOST;
+    const size_t cost_bytes = N * L * sizeof(int32_t), table_bytes = (size_t)L * L * sizeof(int32_t);
+    const size_t lab = N * sizeof(int32_t);
+    Arena a;
+    const size_t id_d = host ? a.add(cost_bytes) : 0;
+    const size_t id_v = host ? a.add(table_bytes) : 0;
+    const size_t id_res = a.add(lab);
+    const size_t id_zero = a.add(8 * lab);  // excess, height, six residue slots: zeroed together
+    const size_t id_scr = a.add(4 * lab);   // newResult, distances, two frontiers
+    const size_t id_st = a.add(64);
+    GINF_TRY(ws_reserve(c.ws, a.total()));
+    unsigned char *base = c.ws->arena;
+    cudaStream_t s = c.r.stream;
+    AlphaBetaParams p{};
+    p.W = W;
+    p.H = H;
+    p.L = L;
+    p.D = static_cast<const int32_t *>(grid->data_costs);
+    p.V = static_cast<const int32_t *>(grid->sm_costs);
+    if (host) {
+        GINF_CK(cudaMemcpyAsync(a.ptr(base, id_d), grid->data_costs, cost_bytes, cudaMemcpyHostToDevice, s));
+        GINF_CK(cudaMemcpyAsync(a.ptr(base, id_v), grid->sm_costs, table_bytes, cudaMemcpyHostToDevice, s));
+        p.D = reinterpret_cast<const int32_t *>(a.ptr(base, id_d));
+        p.V = reinterpret_cast<const int32_t *>(a.ptr(base, id_v));
+        c.h2d += cost_bytes + table_bytes + lab;
+    }
+    p.result = reinterpret_cast<int32_t *>(a.ptr(base, id_res));
+    int32_t *zero = reinterpret_cast<int32_t *>(a.ptr(base, id_zero));
+    p.excess = zero;
+    p.height = zero + N;
+    p.res = zero + 2 * N;
+    int32_t *scr = reinterpret_cast<int32_t *>(a.ptr(base, id_scr));
+    p.newr = scr;
+    p.dist = scr + N;
+    p.q0 = scr + 2 * N;
+    p.q1 = scr + 3 * N;
+    p.iters = iters;
+    p.status = reinterpret_cast<int *>(a.ptr(base, id_st));
+    GINF_CK(cudaMemcpyAsync(p.result, initial, lab, host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+    // The reference's excess, height and residue matrices start at zero
+    // (src/matrix.cc:21-27) and keep their values from one label pair to the
+    // next.
+    GINF_CK(cudaMemsetAsync(zero, 0, 8 * lab, s));
+    GINF_CK(cudaMemsetAsync(p.status, 0, sizeof(int), s));
+    c.ev(EV_UPLOAD);
+    c.ev(EV_PREPARE);
+    c.ev(EV_L0_START);
+    c.ev(EV_SWEEPS);
+    GINF_CK(launch_alpha_beta(p, s));
+    ++c.launches;
+    c.ev(EV_ICM);
+    c.ev(EV_ENERGY);
+    GINF_CK(cudaMemcpyAsync(result, p.result, lab, host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+    if (host) c.d2h += lab;
+    c.ev(EV_END);
+    GINF_CK(cudaMemcpyAsync(c.ws->status_host, p.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GINF_CK(cudaStreamSynchronize(s));
+    GINF_TRY(device_status_error(*c.ws->status_host));
+    return finish(c, 0);
+}
+
 ginf_status ginf_energy(ginf_workspace *wsp, const ginf_grid *grid, const int32_t *labels, double *energy,
                         const ginf_options *opt) {
     g_last_error.clear();

@@ -2,7 +2,8 @@
 //
 // Matrix / Grid re-implement src/matrix.cc and src/grid.cc; the solver entry
 // points that the reference defines in src/bp.cc, src/gpu/bp.cu, src/icm.cc
-// and src/gpu/icm.cu forward to ginf_decode_hbp / ginf_decode_icm, and
+// and src/gpu/icm.cu forward to ginf_decode_hbp / ginf_decode_icm, the
+// alpha-beta swap of src/graphcut.cc to ginf_decode_alpha_beta, and
 // Grid::getLabelingCost(f) (src/grid.cc:102-125) to ginf_energy.  Explicit
 // instantiations for float and int match the reference's.
 #include <cstdarg>
@@ -11,6 +12,7 @@
 #include <cstring>
 
 #include "ginf/bp.h"
+#include "ginf/graphcut.h"
 #include "ginf/icm.h"
 #include "ginf_gb300.h"
 
@@ -287,6 +289,23 @@ template <typename T>
 void decodeIcmAsync(Grid<T> *grid, Matrix<int> *initial, int numIters, Matrix<int> *result) {
     icm(grid, initial, numIters, result, 1, "decodeIcmAsync");
 }
+
+template <typename T>
+void decodeAlphaBeta(Grid<T> *grid, Matrix<int> *initial, int numIters, Matrix<int> *result) {
+    const int64_t n = (int64_t)grid->getWidth() * grid->getHeight();
+    if (!check_labels(initial, n, "decodeAlphaBeta") || !check_labels(result, n, "decodeAlphaBeta")) return;
+    ginf_grid c = to_c(grid);
+    report(ginf_decode_alpha_beta(t_ws.get(), &c, initial->data, numIters, result->data, nullptr, nullptr),
+           "decodeAlphaBeta");
+}
+
+template <typename T>
+void gpuDecodeAlphaBeta(Grid<T> *grid, Matrix<int> *initial, int numIters, Matrix<int> *result) {
+    decodeAlphaBeta(grid, initial, numIters, result);
+}
+
+template void decodeAlphaBeta<int>(Grid<int> *, Matrix<int> *, int, Matrix<int> *);
+template void gpuDecodeAlphaBeta<int>(Grid<int> *, Matrix<int> *, int, Matrix<int> *);
 
 template void decodeHbp<float>(Grid<float> *, int, int, Matrix<int> *);
 template void decodeHbp<int>(Grid<int> *, int, int, Matrix<int> *);

@@ -207,6 +207,19 @@ cudaError_t launch_project_fine(const RecordFormat &f, const unsigned char *rec0
 cudaError_t launch_warm_init(const RecordFormat &f, unsigned char *rec, int W, int H, const float *y, const float *x,
                              float factor, cudaStream_t s);
 
+// Alpha-beta swap (graphcut.cu): int32 costs D (label-planar) and table V on
+// the device; result holds the initial labelling and receives the final one;
+// excess, height and res (6 * W * H, slot-major) must start at zero; newr,
+// dist, q0 and q1 are W * H scratch words each.
+struct AlphaBetaParams {
+    int W, H, L;
+    const int32_t *D, *V;
+    int32_t *result, *newr, *excess, *height, *res, *dist, *q0, *q1;
+    int iters;
+    int *status;
+};
+cudaError_t launch_alpha_beta(const AlphaBetaParams &p, cudaStream_t s);
+
 // Sets the message ginf_last_error() returns on this host thread.
 void set_last_error(const char *msg);
 

@@ -174,6 +174,20 @@ ginf_status ginf_decode_icm(ginf_workspace *ws, const ginf_grid *grid, const int
                             int32_t iters, int32_t asynchronous, int32_t *result,
                             const ginf_options *opt, ginf_stats *stats);
 
+/* Alpha-beta swap, replacing ginf::decodeAlphaBeta (src/graphcut.cc:197-279)
+ * and ginf::gpuDecodeAlphaBeta (src/include/graphcut.h:24-25; its GPU source
+ * src/gpu/graphcut.cu does not compile): for up to `iters` passes over every
+ * label pair alpha < beta, the min cut of the pair's graph by push-relabel,
+ * the swap kept when it lowers the energy; stops after a pass without a
+ * change.  int32 grids only (the reference instantiates it for int,
+ * graphcut.cc:281).  The results are the reference's bit for bit, including
+ * its raster-order pushes and relabels and the state it keeps across label
+ * pairs.  result (W*H) receives a copy of initial, then the swaps.  One CTA
+ * runs the whole solve; a solve that runs longer than 60 s on the device
+ * returns GINF_ERR_TIMEOUT. */
+ginf_status ginf_decode_alpha_beta(ginf_workspace *ws, const ginf_grid *grid, const int32_t *initial,
+                                   int32_t iters, int32_t *result, const ginf_options *opt, ginf_stats *stats);
+
 /* Energy of a labelling, ginf::Grid<T>::getLabelingCost(Matrix<int>*)
  * (src/grid.cc:102-125): interior nodes' data terms plus their N and E edges,
  * summed in FP64 on the device (deterministic order). */

@@ -90,6 +90,8 @@ def lib():
         L.orc_energy_f64.restype = _d
         L.orc_energy_i32_f64.argtypes = [_i, _i, _i, _p, _p, _p]
         L.orc_energy_i32_f64.restype = _d
+        L.orc_alpha_beta_i32.argtypes = [_i, _i, _i, _p, _p, _p, _i, _p]
+        L.orc_alpha_beta_i32.restype = _i
         L.orc_pyramid_f32.argtypes = [_i, _i, _i, _p, _p]
         L.orc_send_linear_f32.argtypes = [_i, _p, _p, _f, _f, _p]
         L.orc_dt_quad_f64.argtypes = [_i, _p, _d, _p]
@@ -117,6 +119,7 @@ def ref():
         R.ref_energy_f32.restype = _f
         R.ref_energy_i32.argtypes = [_i, _i, _i, _p, _i, _i, _i, _p, _p]
         R.ref_energy_i32.restype = ctypes.c_int32
+        R.ref_alpha_beta_i32.argtypes = [_i, _i, _i, _p, _i, _i, _i, _p, _p, _i, _p]
         _ref = R
     return _ref
 
@@ -260,6 +263,29 @@ def ref_icm(D, V, model, scale, d, initial, iters, asynchronous=False):
     out = np.zeros((H, W), np.int32)
     getattr(R, "ref_icm_" + k)(W, H, L, _ptr(D), model, scale, d, _ptr(V), _ptr(_c32(initial, np.int32)), iters,
                                _ptr(out), int(asynchronous))
+    return out
+
+
+def ref_alpha_beta(D, V, model, scale, d, initial, iters):
+    """The reference's decodeAlphaBeta<int> (src/graphcut.cc:197-279)."""
+    R = ref()
+    D = _c32(D, np.int32)
+    V = _c32(V, np.int32)
+    W, H, L = _dims(D)
+    out = np.zeros((H, W), np.int32)
+    R.ref_alpha_beta_i32(W, H, L, _ptr(D), model, int(scale), int(d), _ptr(V), _ptr(_c32(initial, np.int32)),
+                         iters, _ptr(out))
+    return out
+
+
+def alpha_beta(D, V, initial, iters):
+    """Alpha-beta swap restated in C (int grids; src/graphcut.cc:197-279)."""
+    D = _c32(D, np.int32)
+    V = _c32(V, np.int32)
+    W, H, L = _dims(D)
+    out = np.zeros((H, W), np.int32)
+    rc = lib().orc_alpha_beta_i32(W, H, L, _ptr(D), _ptr(V), _ptr(_c32(initial, np.int32)), iters, _ptr(out))
+    assert rc == 0
     return out
 
 

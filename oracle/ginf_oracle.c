@@ -345,3 +345,198 @@ int orc_hbp_f64_std(int W, int H, int L, const float *D, const float *Vf, int mo
     free(V);
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Alpha-beta swap by push-relabel max-flow, src/graphcut.cc:9-279 (int      */
+/* grids only, graphcut.cc:281).  Restated statement by statement in the     */
+/* reference's order, including what it carries from one label pair to the  */
+/* next: nodes outside the alpha-beta partition keep the excess, height and  */
+/* residues their last pair left (graphCutConstructGraph, :10-45, rewrites   */
+/* only partition nodes), and those still take part in the active count, the */
+/* relabels, the pushes and the reachability.  Residues per node: the four   */
+/* directions, then the source slot (never used) and the sink slot,          */
+/* slot-major (s * N + node) as the reference's Matrix(3, W, H, 6).          */
+
+#define GC_SINK 5
+#define GC_ITERS_PER_RELABEL 10 /* GINF_GRAPHCUT_NUM_ITERS_PER_GLOBAL_RELABEL, graphcut.h:8 */
+
+static int gc_valid(int x, int y, int W, int H) { return x >= 0 && y >= 0 && x < W && y < H; }
+
+/* graphCutConstructGraph, graphcut.cc:10-45 (residue plays the capacity). */
+static void gc_construct(int W, int H, int L, const int32_t *D, const int32_t *V, const int32_t *f,
+                         int32_t *height, int32_t *excess, int32_t *res, int alpha, int beta)
+{
+    const size_t N = (size_t)W * H;
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++) {
+            const size_t p = (size_t)y * W + x;
+            if (f[p] != alpha && f[p] != beta) continue;
+            int32_t ac = 0, bc = 0;
+            for (int d = 0; d < 4; d++) {
+                const int nx = x + ORC_DX[d], ny = y + ORC_DY[d];
+                if (gc_valid(nx, ny, W, H)) {
+                    const int fn = f[(size_t)ny * W + nx];
+                    if (fn == alpha || fn == beta) {
+                        res[d * N + p] = V[alpha + (size_t)L * beta];
+                    } else {
+                        res[d * N + p] = 0;
+                        ac += V[alpha + (size_t)L * fn];
+                        bc += V[beta + (size_t)L * fn];
+                    }
+                } else {
+                    res[d * N + p] = 0;
+                }
+            }
+            excess[p] = D[p + N * (size_t)alpha] + ac;
+            res[GC_SINK * N + p] = D[p + N * (size_t)beta] + bc;
+            height[p] = 0;
+        }
+}
+
+/* graphCutGlobalRelabel, graphcut.cc:91-140: breadth-first distances to the
+ * sink over residual edges (a FIFO from the sink-adjacent nodes in raster
+ * order); unreachable nodes get max(height, N + 2). */
+static void gc_global_relabel(int W, int H, int32_t *height, const int32_t *res, int32_t *h, int32_t *queue)
+{
+    const size_t N = (size_t)W * H;
+    size_t head = 0, tail = 0;
+    for (size_t p = 0; p < N; p++) {
+        h[p] = 0;
+        if (res[GC_SINK * N + p]) {
+            h[p] = 1;
+            queue[tail++] = (int32_t)p;
+        }
+    }
+    while (head < tail) {
+        const int32_t p = queue[head++];
+        const int x = p % W, y = p / W;
+        for (int d = 0; d < 4; d++) {
+            const int nx = x + ORC_DX[d], ny = y + ORC_DY[d];
+            if (!gc_valid(nx, ny, W, H)) continue;
+            const size_t q = (size_t)ny * W + nx;
+            if (res[ORC_OPP(d) * N + q] && h[q] == 0) {
+                h[q] = h[p] + 1;
+                queue[tail++] = (int32_t)q;
+            }
+        }
+    }
+    for (size_t p = 0; p < N; p++) {
+        if (h[p] == 0) h[p] = height[p] > (int32_t)N + 2 ? height[p] : (int32_t)N + 2;
+        height[p] = h[p];
+    }
+}
+
+/* graphCutPush / graphCutPushToPixel, graphcut.cc:143-177. */
+static void gc_push(int W, int H, const int32_t *height, int32_t *excess, int32_t *res, int x, int y)
+{
+    const size_t N = (size_t)W * H, p = (size_t)y * W + x;
+    if (!(excess[p] && height[p] < (int32_t)N + 2)) return;
+    if (res[GC_SINK * N + p] && height[p] == 1) {
+        const int32_t flow = ORC_MIN(res[GC_SINK * N + p], excess[p]);
+        excess[p] -= flow;
+        res[GC_SINK * N + p] -= flow;
+    }
+    for (int d = 0; d < 4; d++) {
+        if (res[d * N + p] && height[p] == height[(size_t)(y + ORC_DY[d]) * W + x + ORC_DX[d]] + 1) {
+            const size_t q = (size_t)(y + ORC_DY[d]) * W + x + ORC_DX[d];
+            const int32_t flow = ORC_MIN(res[d * N + p], excess[p]);
+            excess[p] -= flow;
+            excess[q] += flow;
+            res[d * N + p] -= flow;
+            res[ORC_OPP(d) * N + q] += flow;
+        }
+    }
+}
+
+/* graphCutRelabel, graphcut.cc:180-195. */
+static void gc_relabel(int W, int H, int32_t *height, const int32_t *excess, const int32_t *res, int x, int y)
+{
+    const size_t N = (size_t)W * H, p = (size_t)y * W + x;
+    if (!(excess[p] && height[p] < (int32_t)N + 2)) return;
+    if (res[GC_SINK * N + p]) {
+        height[p] = 1;
+    } else {
+        int32_t mh = (int32_t)N + 2;
+        for (int d = 0; d < 4; d++)
+            if (res[d * N + p]) mh = ORC_MIN(mh, height[(size_t)(y + ORC_DY[d]) * W + x + ORC_DX[d]]);
+        height[p] = mh + 1;
+    }
+}
+
+/* graphCutFindReachable from every node with sink residue, graphcut.cc:47-58
+ * and :253-260 (a recursive depth-first search there; the set it marks --
+ * the nodes that reach the sink over residual edges -- is the same for an
+ * explicit stack). */
+static void gc_reachable(int W, int H, const int32_t *res, int32_t *reach, int32_t *stack)
+{
+    const size_t N = (size_t)W * H;
+    memset(reach, 0, sizeof(int32_t) * N);
+    size_t top = 0;
+    for (size_t s = 0; s < N; s++) {
+        if (!res[GC_SINK * N + s] || reach[s]) continue;
+        reach[s] = 1;
+        stack[top++] = (int32_t)s;
+        while (top) {
+            const int32_t p = stack[--top];
+            const int x = p % W, y = p / W;
+            for (int d = 0; d < 4; d++) {
+                const int nx = x + ORC_DX[d], ny = y + ORC_DY[d];
+                if (!gc_valid(nx, ny, W, H)) continue;
+                const size_t q = (size_t)ny * W + nx;
+                if (res[ORC_OPP(d) * N + q] && !reach[q]) {
+                    reach[q] = 1;
+                    stack[top++] = (int32_t)q;
+                }
+            }
+        }
+    }
+}
+
+int orc_alpha_beta_i32(int W, int H, int L, const int32_t *D, const int32_t *V, const int32_t *initial, int iters,
+                       int32_t *result)
+{
+    if (W < 1 || H < 1 || L < 1 || iters < 0) return -1;
+    const size_t N = (size_t)W * H;
+    int32_t *excess = calloc(N, sizeof(int32_t)), *height = calloc(N, sizeof(int32_t));
+    int32_t *res = calloc(N * 6, sizeof(int32_t)), *reach = calloc(N, sizeof(int32_t));
+    int32_t *newr = malloc(N * sizeof(int32_t)), *h = malloc(N * sizeof(int32_t));
+    int32_t *queue = malloc(N * sizeof(int32_t)), *stack = malloc(N * sizeof(int32_t));
+    if (!excess || !height || !res || !reach || !newr || !h || !queue || !stack) return -1;
+    memcpy(result, initial, N * sizeof(int32_t));
+    memcpy(newr, initial, N * sizeof(int32_t));
+    int32_t min_cost = orc_energy_i32_seq(W, H, L, D, V, result);
+    int success = 1;
+    for (int t = 0; t < iters && success; t++) {
+        success = 0;
+        for (int alpha = 0; alpha < L; alpha++)
+            for (int beta = alpha + 1; beta < L; beta++) {
+                gc_construct(W, H, L, D, V, result, height, excess, res, alpha, beta);
+                for (;;) {
+                    size_t active = 0;
+                    for (size_t p = 0; p < N; p++)
+                        if (excess[p] && height[p] < (int32_t)N + 2) active++;
+                    if (active == 0) break;
+                    gc_global_relabel(W, H, height, res, h, queue);
+                    for (int i = 0; i < GC_ITERS_PER_RELABEL; i++) {
+                        for (int y = 0; y < H; y++)
+                            for (int x = 0; x < W; x++) gc_push(W, H, height, excess, res, x, y);
+                        for (int y = 0; y < H; y++)
+                            for (int x = 0; x < W; x++) gc_relabel(W, H, height, excess, res, x, y);
+                    }
+                }
+                gc_reachable(W, H, res, reach, stack);
+                for (size_t p = 0; p < N; p++)          /* graphCutLabelFromFlow, :60-72 */
+                    if (newr[p] == alpha || newr[p] == beta) newr[p] = reach[p] ? alpha : beta;
+                const int32_t cost = orc_energy_i32_seq(W, H, L, D, V, newr);
+                if (cost < min_cost) {
+                    min_cost = cost;
+                    memcpy(result, newr, N * sizeof(int32_t));
+                    success = 1;
+                } else {
+                    memcpy(newr, result, N * sizeof(int32_t));
+                }
+            }
+    }
+    free(excess); free(height); free(res); free(reach); free(newr); free(h); free(queue); free(stack);
+    return 0;
+}

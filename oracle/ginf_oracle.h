@@ -68,6 +68,13 @@ int32_t orc_energy_i32_seq(int W, int H, int L, const int32_t *D, const int32_t 
 double  orc_energy_f64(int W, int H, int L, const float *D, const float *V, const int32_t *f);
 double  orc_energy_i32_f64(int W, int H, int L, const int32_t *D, const int32_t *V, const int32_t *f);
 
+/* Alpha-beta swap, src/graphcut.cc:197-279 (decodeAlphaBeta, int grids):
+ * push-relabel max-flow per label pair in the reference's raster order, with
+ * the state it carries across pairs.  result receives a copy of initial
+ * first.  Returns 0, or -1 on bad input or allocation failure. */
+int orc_alpha_beta_i32(int W, int H, int L, const int32_t *D, const int32_t *V, const int32_t *initial, int iters,
+                       int32_t *result);
+
 /* Building blocks exposed for unit tests. */
 void orc_pyramid_f32(int W, int H, int L, const float *D, float *Dc);   /* bp.cc:100-117 one level */
 void orc_send_linear_f32(int L, const float *from, const float *in, float scale, float trunc, float *out);

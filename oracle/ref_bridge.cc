@@ -1,7 +1,7 @@
 // ref_bridge.cc -- extern "C" entry points into the reference's own CPU code.
 //
 // TEST INFRASTRUCTURE ONLY.  oracle/Makefile compiles this file together with
-// the reference's unmodified src/{grid,matrix,bp,icm}.cc (from the read-only
+// the reference's unmodified src/{grid,matrix,bp,icm,graphcut}.cc (from the read-only
 // reference checkout, never copied) into oracle/_ref/libginf_ref.so.  The
 // tests use it to pin the C restatement (ginf_oracle.c) and to write the
 // golden fixtures under tests/golden/.
@@ -12,6 +12,7 @@
 #include <cstring>
 
 #include "bp.h"
+#include "graphcut.h"
 #include "grid.h"
 #include "icm.h"
 #include "matrix.h"
@@ -122,6 +123,18 @@ T energy(int W, int H, int L, const T *D, int model, T scale, T d, const T *V, c
     return e;
 }
 
+// decodeAlphaBeta (src/graphcut.cc:197-279), instantiated for int only (:281).
+int alpha_beta(int W, int H, int L, const int *D, int model, int scale, int d, const int *V, const int32_t *initial,
+               int iters, int32_t *result) {
+    ginf::Grid<int> *g = make_grid<int>(W, H, L, D, model, scale, d, V);
+    ginf::Matrix<int> init(2, W, H), res(2, W, H);
+    std::memcpy(init.data, initial, sizeof(int) * (size_t)W * H);
+    ginf::decodeAlphaBeta(g, &init, iters, &res);
+    std::memcpy(result, res.data, sizeof(int) * (size_t)W * H);
+    delete g;
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -163,6 +176,11 @@ float ref_energy_f32(int W, int H, int L, const float *D, int model, float scale
 int32_t ref_energy_i32(int W, int H, int L, const int32_t *D, int model, int32_t scale, int32_t d,
                        const int32_t *V, const int32_t *labels) {
     return energy<int>(W, H, L, (const int *)D, model, scale, d, (const int *)V, labels);
+}
+
+int ref_alpha_beta_i32(int W, int H, int L, const int32_t *D, int model, int32_t scale, int32_t d,
+                       const int32_t *V, const int32_t *initial, int iters, int32_t *result) {
+    return alpha_beta(W, H, L, (const int *)D, model, scale, d, (const int *)V, initial, iters, result);
 }
 
 }  // extern "C"

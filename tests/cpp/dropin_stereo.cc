@@ -12,12 +12,14 @@
 //            as a Grid<float> with TruncLinear(1.5, 3): decodeBp (12),
 //            gpuDecodeHbp (2 levels x 5), decodeIcmAsync (2 sweeps) and
 //            gpuDecodeIcm (3 sweeps) from the decodeBp labels, W*H labels
-//            each, and the float energy of the decodeBp labelling.
+//            each, and the float energy of the decodeBp labelling; then the
+//            int grid's gpuDecodeAlphaBeta (1 pass from the BP labels), W*H.
 #include <cstdio>
 #include <vector>
 
 #include "ginf/bp.h"
 #include "ginf/core.h"
+#include "ginf/graphcut.h"
 #include "ginf/icm.h"
 
 // Reference code may size its own buffers or launches with the library's
@@ -71,6 +73,9 @@ int main(int argc, char **argv) {
     if (ginf::lastStatus() != 0) return 1;
     const float fenergy = fgrid.getLabelingCost(&fbp);
     if (ginf::lastStatus() != 0) return 1;
+    ginf::Matrix<int> ab(2, W, H);
+    ginf::gpuDecodeAlphaBeta(&grid, &bp, 1, &ab);
+    if (ginf::lastStatus() != 0) return 1;
 
     FILE *o = std::fopen(argv[2], "wb");
     if (!o) return 2;
@@ -83,6 +88,7 @@ int main(int argc, char **argv) {
     std::fwrite(ficma.data, sizeof(int), (size_t)W * H, o);
     std::fwrite(ficmg.data, sizeof(int), (size_t)W * H, o);
     std::fwrite(&fenergy, sizeof(float), 1, o);
+    std::fwrite(ab.data, sizeof(int), (size_t)W * H, o);
     std::fclose(o);
     return 0;
 }

@@ -74,6 +74,32 @@ def initial_labels(W, H, L, seed):
     return rng.integers(0, L - 1, W * H).reshape(H, W).astype(np.int32)
 
 
+# Alpha-beta swap cases (int grids): (name, W, H, L, seed, model, scale, trunc, iters)
+ALPHA_BETA = [
+    ("ab_lin_23x17_L5", 23, 17, 5, 30, synth.TRUNC_LINEAR, 2, 6, 3),
+    ("ab_potts_31x19_L4", 31, 19, 4, 31, synth.POTTS, 3, 0, 3),
+    ("ab_quad_20x26_L6", 20, 26, 6, 32, synth.TRUNC_QUAD, 1, 9, 2),
+    ("ab_explicit_15x12_L5", 15, 12, 5, 33, synth.EXPLICIT, 0, 0, 2),
+    ("ab_lin_1x9_L3", 1, 9, 3, 34, synth.TRUNC_LINEAR, 1, 2, 2),
+    ("ab_lin_64x48_L8", 64, 48, 8, 35, synth.TRUNC_LINEAR, 10, 20, 2),
+]
+
+
+def alpha_beta_cases(gold, arrays):
+    """The reference's own decodeAlphaBeta<int> (src/graphcut.cc:197-279) on
+    seeded int grids from a seeded initial labelling."""
+    for (name, W, H, L, seed, model, scale, trunc, iters) in ALPHA_BETA:
+        P = synth.random_problem(W, H, L, seed, model=model, scale=scale, trunc=trunc, dtype=np.int32, cost_max=20)
+        init = initial_labels(W, H, L, seed)
+        lab = oracle.ref_alpha_beta(P.D, P.V, model, scale, trunc, init, iters)
+        gold["cases"][name] = dict(kind="alpha_beta", W=W, H=H, L=L, seed=seed, model=model, scale=scale,
+                                   trunc=trunc, dtype="i32", iters=iters, cost_sha=sha(P.D), table_sha=sha(P.V),
+                                   energy_ref_type=int(oracle.ref_energy(P.D, P.V, model, scale, trunc, lab)))
+        arrays[name + "/init"] = init.astype(np.int16)
+        arrays[name + "/labels"] = lab.astype(np.int16)
+        print("case", name, flush=True)
+
+
 def stereo_png_case(gold, arrays):
     """The reference example end to end (examples/stereo/stereo.cc:16-43):
     its own stereo pair as grey images, Grid<int> with L = 16 and costs
@@ -104,19 +130,25 @@ def main():
     ap.add_argument("--skip-large", action="store_true", help="skip the 1920x1080 reference HBP run (minutes)")
     ap.add_argument("--only-stereo-png", action="store_true",
                     help="keep every existing fixture and (re)write only the stereo PNG case")
+    ap.add_argument("--only-alpha-beta", action="store_true",
+                    help="keep every existing fixture and (re)write only the alpha-beta swap cases")
     args = ap.parse_args()
     oracle.build(with_ref=True)
     assert oracle.ref() is not None, "the reference bridge did not build"
-    if args.only_stereo_png:
+    if args.only_stereo_png or args.only_alpha_beta:
         with open(os.path.join(HERE, "golden.json")) as f:
             gold = json.load(f)
         arrays = dict(np.load(os.path.join(HERE, "golden_arrays.npz")))
-        stereo_png_case(gold, arrays)
+        if args.only_stereo_png:
+            stereo_png_case(gold, arrays)
+        if args.only_alpha_beta:
+            alpha_beta_cases(gold, arrays)
         write(gold, arrays)
         return
     gold = {"generator": "tests/golden/make_golden.py", "cases": {}}
     arrays = {}
     stereo_png_case(gold, arrays)
+    alpha_beta_cases(gold, arrays)
 
     for (name, W, H, L, seed, model, scale, trunc, dtype, iters) in SMALL_BP:
         P = small_problem(W, H, L, seed, model, scale, trunc, dtype)

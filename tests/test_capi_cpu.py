@@ -44,6 +44,8 @@ CXX_SIGNATURES = [
     "ginf::Matrix<int>::Matrix(int, ...)",
     "ginf::Matrix<float>::copyFrom(ginf::Matrix<float>*)",
     "ginf::lastStatus()",
+    "ginf::decodeAlphaBeta<int>(ginf::Grid<int>*, ginf::Matrix<int>*, int, ginf::Matrix<int>*)",
+    "ginf::gpuDecodeAlphaBeta<int>(ginf::Grid<int>*, ginf::Matrix<int>*, int, ginf::Matrix<int>*)",
 ]
 
 
@@ -128,8 +130,9 @@ MACRO_PROGRAM = r'''
 #include "ginf/core.h"
 #include "ginf/bp.h"
 #include "ginf/icm.h"
+#include "ginf/graphcut.h"
 // Every macro, enum and constant the reference's public headers define
-// (src/include/{utils,matrix,bp,icm}.h), with the reference's values.
+// (src/include/{utils,matrix,bp,icm,graphcut}.h), with the reference's values.
 static_assert(GINF_BP_BLOCK_WIDTH == 32 && GINF_BP_BLOCK_HEIGHT == 4, "bp.h:8-9");
 static_assert(GINF_ICM_BLOCK_SIZE == 16, "icm.h:8");
 static_assert(GINF_MAT_MAX_NUM_DIMS == 4, "matrix.h:6");
@@ -140,6 +143,9 @@ static_assert(GINF_IS_VALID_NODE(0, 0, 1, 1) && !GINF_IS_VALID_NODE(1, 0, 1, 1),
 static_assert(GINF_MIN(3, 4) == 3 && GINF_MAX(3, 4) == 4 && GINF_ABS(-5) == 5 && GINF_SQ(-3) == 9, "utils.h:16-19");
 static_assert(GINF_MAX_NUM_LABELS >= 16, "utils.h:22 (raised to 128 here)");
 static_assert(ginf::GINF_SM_EXPLICIT == 0 && ginf::GINF_SM_TRUNC_QUAD == 3, "grid.h:9-14");
+static_assert(GINF_GRAPHCUT_NUM_ITERS_PER_GLOBAL_RELABEL == 10 && GINF_GRAPHCUT_BLOCK_WIDTH == 32 &&
+              GINF_GRAPHCUT_BLOCK_HEIGHT == 8 && GINF_GRAPHCUT_NUM_THREADS_PER_BLOCK == 256, "graphcut.h:8-11");
+static_assert(ginf::GINF_DIR_SOURCE == 4 && ginf::GINF_DIR_SINK == 5, "graphcut.h:14-17");
 int main() {
     int block[2] = {GINF_BP_BLOCK_WIDTH, GINF_BP_BLOCK_HEIGHT};
     int s = 0;

@@ -36,6 +36,7 @@ def test_cpp_program_matches_oracle(ginf, orc, built_lib, tmp_path):
     f = res[3 * n + 1:]
     fbp, fhbp, ficma, ficmg = (f[i * n:(i + 1) * n].reshape(H, W) for i in range(4))
     fenergy = f[4 * n:4 * n + 1].view(np.float32)[0]
+    ab = f[4 * n + 1:5 * n + 1].reshape(H, W)
     V = synth.sm_table(L, synth.TRUNC_LINEAR, 10, 20, dtype=np.int32)
     want_bp, _ = orc.hbp(D, V, synth.TRUNC_LINEAR, 1, 30)
     want_hbp, _ = orc.hbp(D, V, synth.TRUNC_LINEAR, 3, 6)
@@ -43,6 +44,7 @@ def test_cpp_program_matches_oracle(ginf, orc, built_lib, tmp_path):
     assert np.array_equal(hbp, want_hbp)
     assert np.array_equal(icm, orc.icm(D, V, want_bp, 2))
     assert energy == orc.energy(D, V, want_bp, exact_type=True)
+    assert np.array_equal(ab, orc.alpha_beta(D, V, want_bp, 1))   # gpuDecodeAlphaBeta<int>
     # The same costs as a Grid<float>: decodeBp, gpuDecodeHbp, decodeIcmAsync, gpuDecodeIcm.
     Df = (np.float32(0.25) * D.astype(np.float32)).astype(np.float32)
     Vf = synth.sm_table(L, synth.TRUNC_LINEAR, 1.5, 3.0)

@@ -177,3 +177,34 @@ def test_fp64_standard_oracle_equals_reference_on_linear(orc):
     l32, _ = orc.hbp(P.D, P.V, P.model, 1, 20)
     l64, _ = orc.hbp_f64_std(P.D, P.V, P.model, 1, 20)
     assert (l32 == l64).mean() > 0.99
+
+
+@pytest.mark.parametrize("W,H,L,seed,model,scale,trunc,iters", [
+    (9, 7, 3, 1, synth.TRUNC_LINEAR, 1, 2, 2), (17, 13, 4, 2, synth.POTTS, 3, 0, 3),
+    (20, 15, 5, 3, synth.TRUNC_LINEAR, 2, 6, 2), (12, 10, 6, 4, synth.EXPLICIT, 0, 0, 2),
+    (1, 8, 3, 5, synth.TRUNC_LINEAR, 1, 3, 2), (8, 1, 2, 6, synth.POTTS, 2, 0, 2), (2, 2, 2, 7, synth.POTTS, 1, 0, 3),
+    (31, 23, 8, 8, synth.TRUNC_LINEAR, 3, 9, 3), (40, 30, 4, 9, synth.TRUNC_QUAD, 1, 9, 2),
+    (25, 19, 5, 10, synth.TRUNC_LINEAR, 2, 6, 0)])
+def test_alpha_beta_oracle_vs_reference(orc, W, H, L, seed, model, scale, trunc, iters):
+    """The C restatement of the alpha-beta swap (graphcut.cc:197-279) against
+    the reference's own compiled decodeAlphaBeta<int>, bit for bit, from a
+    random initial labelling."""
+    _need_ref(orc)
+    P = synth.random_problem(W, H, L, seed, model=model, scale=scale, trunc=trunc, dtype=np.int32, cost_max=20)
+    init = synth.Rng(seed, 5).integers(0, L - 1, W * H).reshape(H, W).astype(np.int32)
+    ref = orc.ref_alpha_beta(P.D, P.V, model, scale, trunc, init, iters)
+    assert np.array_equal(orc.alpha_beta(P.D, P.V, init, iters), ref)
+
+
+def test_oracle_matches_golden_alpha_beta(orc, golden):
+    """The alpha-beta fixtures the reference wrote (tests/golden), reproduced
+    by the C restatement without the reference checkout."""
+    meta, arr = golden
+    cases = [(n, c) for n, c in meta["cases"].items() if c["kind"] == "alpha_beta"]
+    assert len(cases) >= 5
+    for name, case in cases:
+        P = golden_problem(case)
+        assert sha(P.D) == case["cost_sha"], name
+        lab = orc.alpha_beta(P.D, P.V, arr[name + "/init"].astype(np.int32), case["iters"])
+        assert np.array_equal(lab, arr[name + "/labels"]), name
+        assert orc.energy(P.D, P.V, lab, exact_type=True) == case["energy_ref_type"], name
