@@ -49,6 +49,7 @@ WORKLOADS = {
     "warm": dict(name="learned_warm_start_hbp_1920x1080_L64", W=1920, H=1080, L=64, levels=5, iters=0, icm=0),
     "batch": dict(name="batch64_lbp_200x150-1280x720_L16-64_30it", W=0, H=0, L=0, levels=1, iters=30, icm=0,
                   count=64),
+    "alphabeta": dict(name="alpha_beta_384x288_L16_int_1pass", W=384, H=288, L=16, levels=1, iters=1, icm=0),
 }
 METRIC = "node-label-iters/s (LBP)"
 UNIT = "node*label*iter/s"
@@ -756,6 +757,73 @@ def run_warm(args, cfg):
     net.close()
 
 
+# ---------------------------------------------------------------- alpha-beta swap
+
+def run_alphabeta(args, cfg):
+    """Alpha-beta swap (src/graphcut.cc:197-279) on the reference example's
+    integer problem shape: 8-bit grey images of the seeded 384x288 stereo
+    pair, costs min(|L(x) - R(x-k)|, 20) for x >= L-1 (ginf_stereo_costs_u8),
+    TruncLinear(10, 20), 16 labels, from the 30-iteration loopy-BP labels,
+    `iters` passes.  One step is one solve from device buffers; the oracle's
+    C restatement (single-threaded, as the reference) is timed on the same
+    input and its labels compared."""
+    import hashlib
+    import numpy as np
+    import torch
+    from gridinfcuda_gb300 import capi, synth
+    torch.cuda.set_device(0)
+    W, H, L, iters = cfg["W"], cfg["H"], cfg["L"], cfg["iters"]
+    pair = synth.stereo_pair(W, H, L, 12, 2.0, seed=0)
+    left = np.clip(np.rint(pair.left), 0, 255).astype(np.uint8)
+    right = np.clip(np.rint(pair.right), 0, 255).astype(np.uint8)
+    D = torch.empty((L, H, W), dtype=torch.int32, device="cuda")
+    capi.stereo_costs_u8(torch.from_numpy(left).cuda(), torch.from_numpy(right).cuda(), L, 20, D)
+    V = torch.from_numpy(synth.sm_table(L, synth.TRUNC_LINEAR, 10, 20, dtype=np.int32)).cuda()
+    init = torch.zeros((H, W), dtype=torch.int32, device="cuda")
+    capi.decode_hbp(D, V, synth.TRUNC_LINEAR, 1, 30, labels=init)
+    ws = capi.Workspace()
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        capi.decode_alpha_beta(D, V, synth.TRUNC_LINEAR, init, iters, workspace=ws, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        out = capi.decode_alpha_beta(D, V, synth.TRUNC_LINEAR, init, iters, workspace=ws, stream=stream.cuda_stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    got = out.cpu().numpy()
+    e0 = capi.energy(D, V, synth.TRUNC_LINEAR, init, workspace=ws)
+    e1 = capi.energy(D, V, synth.TRUNC_LINEAR, out, workspace=ws)
+    pairs = L * (L - 1) // 2
+    line = {"metric": "alpha-beta swap node*pair/s", "value": W * H * pairs * iters / (ms / 1e3),
+            "unit": "node*pair/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32", "data": "synthetic (seeded stereo pair as 8-bit grey images; no dataset)",
+            "config": {"workload": cfg["name"], "width": W, "height": H, "labels": L, "passes": iters,
+                       "costs": "min(|L(x)-R(x-k)|, 20) for x >= L-1", "smoothness": "min(10|a-b|, 20)",
+                       "initial": "30-iteration loopy BP labels"},
+            "energy_initial": e0, "energy": e1, "labels_changed": int((got != init.cpu().numpy()).sum()),
+            "gpu_launches": 1}
+    if not args.no_cpu_baseline:
+        import oracle
+        oracle.build()
+        Dh, Vh, ih = D.cpu().numpy(), V.cpu().numpy(), init.cpu().numpy()
+        t0 = time.perf_counter()
+        want = oracle.alpha_beta(Dh, Vh, ih, iters)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": W * H * pairs * iters / dt, "unit": "node*pair/s", "cores": 1,
+                                "kind": "port", "sample": f"one full solve, {dt:.2f} s (the reference is "
+                                                          f"single-threaded)"}
+        line["cpu_baseline"].update(host_description())
+        line["parity"] = {"ok": bool(np.array_equal(got, want)),
+                          "labels_sha": hashlib.sha256(got.tobytes()).hexdigest()[:16],
+                          "against": "oracle C restatement of src/graphcut.cc (bit-identical to the reference)"}
+    print(json.dumps(line), flush=True)
+    ws.close()
+
+
 # ---------------------------------------------------------------- reference arm
 
 def run_reference(args, cfg):
@@ -830,6 +898,10 @@ def main():
         import gridinfcuda_gb300
         gridinfcuda_gb300.build()
         run_batch(args, cfg)
+    elif args.workload == "alphabeta":
+        import gridinfcuda_gb300
+        gridinfcuda_gb300.build()
+        run_alphabeta(args, cfg)
     elif args.workload == "quad":
         import gridinfcuda_gb300
         gridinfcuda_gb300.build()

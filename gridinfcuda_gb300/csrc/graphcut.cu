@@ -50,7 +50,33 @@ struct Shared {
     int min_cost;
     int success;
     int stop;
+    int kmin, kmax;  // diagonals holding active nodes
 };
+
+// Active nodes (non-zero excess, height below N + 2) as the range of
+// diagonals x + y that hold them: kmin > kmax when there are none.
+__device__ void active_diagonals(const AlphaBetaParams &p, Shared &sh) {
+    const int W = p.W;
+    const size_t N = (size_t)W * p.H;
+    const int32_t NP2 = (int32_t)N + 2;
+    if (threadIdx.x == 0) {
+        sh.kmin = 0x7fffffff;
+        sh.kmax = -1;
+    }
+    __syncthreads();
+    int lo = 0x7fffffff, hi = -1;
+    for (size_t i = threadIdx.x; i < N; i += blockDim.x)
+        if (p.excess[i] && p.height[i] < NP2) {
+            const int k = (int)(i % W) + (int)(i / W);
+            lo = min(lo, k);
+            hi = max(hi, k);
+        }
+    if (hi >= 0) {
+        atomicMin(&sh.kmin, lo);
+        atomicMax(&sh.kmax, hi);
+    }
+    __syncthreads();
+}
 
 // Sum of v over the block, in int32 (wrapping, as the reference's int sums).
 __device__ int block_sum(int v, Shared &sh) {
@@ -196,8 +222,15 @@ __global__ void __launch_bounds__(kThreadsAB, 1) k_alpha_beta(const AlphaBetaPar
                     }
                     __syncthreads();
                     for (int r = 0; r < kItersPerRelabel; ++r) {
+                        // A sweep changes only active nodes and the nodes they
+                        // push into, so it can start at the first diagonal with
+                        // an active node and stop after the last one that holds
+                        // or has received flow; with no active node the rest of
+                        // the ten sweeps change nothing and are left out.
+                        active_diagonals(p, sh);
+                        if (sh.kmin > sh.kmax) break;
                         // Pushes (graphcut.cc:143-177), raster order as wavefronts.
-                        for (int k = 0; k <= W + H - 2; ++k) {
+                        for (int k = sh.kmin; k <= sh.kmax; ++k) {
                             const int xlo = k - (H - 1) > 0 ? k - (H - 1) : 0;
                             const int xhi = k < W - 1 ? k : W - 1;
                             for (int x = xlo + (int)threadIdx.x; x <= xhi; x += blockDim.x) {
@@ -221,13 +254,19 @@ __global__ void __launch_bounds__(kThreadsAB, 1) k_alpha_beta(const AlphaBetaPar
                                     atomicAdd(&ex[q], fl);
                                     res[d * N + i] = rd - fl;
                                     res[gopp(d) * N + q] += fl;
+                                    // South and east neighbours lie on the next
+                                    // diagonal, which this sweep reaches later.
+                                    if (d <= 1) atomicMax(&sh.kmax, k + 1);
                                 }
                                 ex[i] = e;
                             }
                             __syncthreads();
                         }
-                        // Relabels (graphcut.cc:180-195), raster order as wavefronts.
-                        for (int k = 0; k <= W + H - 2; ++k) {
+                        // Relabels (graphcut.cc:180-195), raster order as
+                        // wavefronts: they change only active nodes' heights and
+                        // no excess, so the active diagonals bound them.
+                        active_diagonals(p, sh);
+                        for (int k = sh.kmin; k <= sh.kmax; ++k) {
                             const int xlo = k - (H - 1) > 0 ? k - (H - 1) : 0;
                             const int xhi = k < W - 1 ? k : W - 1;
                             for (int x = xlo + (int)threadIdx.x; x <= xhi; x += blockDim.x) {
