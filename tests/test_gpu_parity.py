@@ -136,6 +136,20 @@ def test_fp64_path_matches_fp64_oracle(ginf, orc):
     assert (got[1:-1, 1:-1] == want[1:-1, 1:-1]).mean() == 1.0
 
 
+def test_fp64_path_on_the_precision_workload_recipe(ginf, orc):
+    """The FP64 path that the precision sweep measures FP32 and FP16 against,
+    on that workload's own recipe (80 slanted planes, sigma 3, L = 128,
+    D = 0.05 min(|dI|, 20), V = min((a-b)^2, 25)) at 384x216, for the sweep's
+    full 40 half-sweeps: messages within 1e-12 of the CPU FP64 oracle and
+    identical labels."""
+    P = synth.workload_quad(seed=3, W=384, H=216, L=128)
+    want, mw = orc.hbp_f64_std(P.D, P.V, P.model, 1, 40, want_msgs=True)
+    got, mg = ginf.decode_hbp(P.D, P.V, P.model, 1, 40, want_msgs=True, compute_type=ginf.F64,
+                              rule=ginf.RULE_STANDARD)
+    assert _msg_rel_err(mg, mw) < 1e-12
+    assert np.array_equal(got[1:-1, 1:-1], want[1:-1, 1:-1])
+
+
 def test_standard_quadratic_fp32_and_fp16_vs_fp64_oracle(ginf, orc):
     """Truncated-quadratic standard BP against the FP64 oracle: messages within
     1e-4 (FP32 store) / 5e-3 (FP16 store) relative; labels agree on >= 99.9% /
