@@ -533,3 +533,29 @@ def test_cluster_launch_schedule(ginf):
     assert st["level0_sweep_launches"] == 8
     _, st1 = ginf.decode_hbp(_dev(P.D), _dev(P.V), P.model, 1, 50, want_stats=True)
     assert st1["level0_sweep_launches"] == 50
+
+
+def test_linear_minimum_with_negative_zero_and_infinite_costs(ginf, orc):
+    """The truncated-linear update keeps the reference's (a < b) ? a : b
+    minimum (GINF_MIN, utils.h:16) on every input: -0 costs give the oracle's
+    messages bit for bit, and infinite costs -- which make NaN messages, where
+    that minimum and min.f32 differ -- give the oracle's labels, NaN in the
+    same slots and the same finite messages."""
+    P = synth.random_problem(41, 29, 8, 77, model=synth.TRUNC_LINEAR, scale=1.0, trunc=2.5)
+    D = P.D.copy()
+    D[:, 3:9, 4:12] = np.float32(-0.0)
+    lab, m = ginf.decode_hbp(_dev(D), _dev(P.V), P.model, 1, 9, want_msgs=True)
+    want, mw = orc.hbp(D, P.V, P.model, 1, 9, want_msgs=True)
+    assert np.array_equal(lab.cpu().numpy(), want)
+    assert np.array_equal(m.cpu().numpy().view(np.uint32), mw.view(np.uint32))
+    D = P.D.copy()
+    D[2, 10, 7] = np.float32(np.inf)
+    D[:, 20, 30] = np.float32(np.inf)
+    lab, m = ginf.decode_hbp(_dev(D), _dev(P.V), P.model, 1, 9, want_msgs=True)
+    want, mw = orc.hbp(D, P.V, P.model, 1, 9, want_msgs=True)
+    m = m.cpu().numpy()
+    assert np.isnan(mw).any()
+    assert np.array_equal(lab.cpu().numpy(), want)
+    assert np.array_equal(np.isnan(m), np.isnan(mw))
+    fin = ~np.isnan(mw)
+    assert np.array_equal(m[fin], mw[fin])
