@@ -165,3 +165,34 @@ def test_reference_macros_compile_against_headers(tmp_path):
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert subprocess.run([str(exe)]).returncode == 0
+
+
+def test_new_entry_points_validate_without_device(built_lib):
+    """Argument errors of the alpha-beta swap, the integer stereo costs and
+    the half-sweeps-per-launch option are reported before any device work."""
+    import numpy as np
+    from gridinfcuda_gb300 import capi
+    L = capi.lib()
+    D = np.zeros((4, 6, 5), np.float32)
+    V = np.zeros(16, np.float32)
+    lab = np.zeros((6, 5), np.int32)
+    g = capi.Grid(5, 6, 4, capi.F32, capi.TRUNC_LINEAR, capi.HOST, D.ctypes.data, V.ctypes.data)
+    # the swap takes int32 grids only, as the reference instantiates it
+    assert L.ginf_decode_alpha_beta(None, ctypes.byref(g), lab.ctypes.data, 1, lab.ctypes.data, None,
+                                    None) == capi.ERR_UNSUPPORTED
+    assert b"int" in L.ginf_last_error()
+    Di, Vi = D.astype(np.int32), V.astype(np.int32)
+    gi = capi.Grid(5, 6, 4, capi.I32, capi.TRUNC_LINEAR, capi.HOST, Di.ctypes.data, Vi.ctypes.data)
+    assert L.ginf_decode_alpha_beta(None, ctypes.byref(gi), None, 1, lab.ctypes.data, None,
+                                    None) == capi.ERR_INVALID_ARGUMENT
+    assert L.ginf_decode_alpha_beta(None, ctypes.byref(gi), lab.ctypes.data, -1, lab.ctypes.data, None,
+                                    None) == capi.ERR_INVALID_ARGUMENT
+    img = np.zeros((6, 5), np.uint8)
+    assert L.ginf_stereo_costs_u8(5, 6, 4, capi.HOST, img.ctypes.data, None, 20, Di.ctypes.data,
+                                  None) == capi.ERR_INVALID_ARGUMENT
+    assert L.ginf_stereo_costs_u8(0, 6, 4, capi.HOST, img.ctypes.data, img.ctypes.data, 20, Di.ctypes.data,
+                                  None) == capi.ERR_INVALID_ARGUMENT
+    o = capi.options(sweeps_per_launch=-2)
+    assert L.ginf_decode_hbp(None, ctypes.byref(g), 1, 2, lab.ctypes.data, ctypes.byref(o),
+                             None) == capi.ERR_INVALID_ARGUMENT
+    assert b"sweeps_per_launch" in L.ginf_last_error()
