@@ -43,6 +43,10 @@ __device__ __forceinline__ int gdx(int d) { return d == 1 ? 1 : (d == 3 ? -1 : 0
 __device__ __forceinline__ int gdy(int d) { return d == 0 ? 1 : (d == 2 ? -1 : 0); }  // utils.h:37
 __device__ __forceinline__ int gopp(int d) { return d >= 2 ? d - 2 : d + 2; }          // utils.h:10
 
+// Diagonals a sweep must visit, one bit each, for grids with W + H - 1 up to
+// kDiagBits (larger grids visit every diagonal of the active range).
+constexpr int kDiagBits = 65536;
+
 struct Shared {
     int red[kThreadsAB / 32];
     int count;      // active nodes / queue tail
@@ -51,7 +55,12 @@ struct Shared {
     int success;
     int stop;
     int kmin, kmax;  // diagonals holding active nodes
+    unsigned diag[kDiagBits / 32];  // diagonals holding active nodes or receiving flow
 };
+
+__device__ __forceinline__ bool diag_visit(const Shared &sh, int k, bool bits) {
+    return !bits || ((sh.diag[k >> 5] >> (k & 31)) & 1u);
+}
 
 // Active nodes (non-zero excess, height below N + 2) as the range of
 // diagonals x + y that hold them: kmin > kmax when there are none.
@@ -59,10 +68,14 @@ __device__ void active_diagonals(const AlphaBetaParams &p, Shared &sh) {
     const int W = p.W;
     const size_t N = (size_t)W * p.H;
     const int32_t NP2 = (int32_t)N + 2;
+    const int nd = W + p.H - 1;
+    const bool bits = nd <= kDiagBits;
     if (threadIdx.x == 0) {
         sh.kmin = 0x7fffffff;
         sh.kmax = -1;
     }
+    if (bits)
+        for (int w = threadIdx.x; w < (nd + 31) / 32; w += blockDim.x) sh.diag[w] = 0u;
     __syncthreads();
     int lo = 0x7fffffff, hi = -1;
     for (size_t i = threadIdx.x; i < N; i += blockDim.x)
@@ -70,6 +83,7 @@ __device__ void active_diagonals(const AlphaBetaParams &p, Shared &sh) {
             const int k = (int)(i % W) + (int)(i / W);
             lo = min(lo, k);
             hi = max(hi, k);
+            if (bits) atomicOr(&sh.diag[k >> 5], 1u << (k & 31));
         }
     if (hi >= 0) {
         atomicMin(&sh.kmin, lo);
@@ -221,42 +235,64 @@ __global__ void __launch_bounds__(kThreadsAB, 1) k_alpha_beta(const AlphaBetaPar
                         ht[i] = h != 0 ? h : (ht[i] > NP2 ? ht[i] : NP2);
                     }
                     __syncthreads();
+                    const bool bits = W + H - 1 <= kDiagBits;
                     for (int r = 0; r < kItersPerRelabel; ++r) {
                         // A sweep changes only active nodes and the nodes they
-                        // push into, so it can start at the first diagonal with
-                        // an active node and stop after the last one that holds
-                        // or has received flow; with no active node the rest of
-                        // the ten sweeps change nothing and are left out.
+                        // push into, so it visits only the diagonals that hold
+                        // an active node or have received flow from the one
+                        // before (the bitmap, read by every thread after the
+                        // last barrier, so the skips are uniform); with no
+                        // active node the rest of the ten sweeps change nothing
+                        // and are left out.
                         active_diagonals(p, sh);
                         if (sh.kmin > sh.kmax) break;
                         // Pushes (graphcut.cc:143-177), raster order as wavefronts.
                         for (int k = sh.kmin; k <= sh.kmax; ++k) {
+                            if (!diag_visit(sh, k, bits)) continue;
                             const int xlo = k - (H - 1) > 0 ? k - (H - 1) : 0;
                             const int xhi = k < W - 1 ? k : W - 1;
                             for (int x = xlo + (int)threadIdx.x; x <= xhi; x += blockDim.x) {
                                 const int y = k - x;
                                 const size_t i = (size_t)y * W + x;
+                                // Everything this push reads, loaded at once: no
+                                // other node touches it while this diagonal runs
+                                // (neighbours lie on diagonals k - 1 and k + 1),
+                                // and its own pushes change distinct slots.
                                 int e = ex[i];
                                 const int h = ht[i];
-                                if (!(e && h < NP2)) continue;
-                                if (res[kSink * N + i] && h == 1) {
-                                    const int fl = min(res[kSink * N + i], e);
-                                    e -= fl;
-                                    res[kSink * N + i] -= fl;
-                                }
+                                int rs = res[kSink * N + i];
+                                int rd[4], hq[4];
+#pragma unroll
                                 for (int d = 0; d < 4; ++d) {
-                                    const int rd = res[d * N + i];
-                                    if (!rd) continue;
+                                    rd[d] = res[d * N + i];
+                                    const int nx = x + gdx(d), ny = y + gdy(d);
+                                    hq[d] = (nx >= 0 && ny >= 0 && nx < W && ny < H) ? ht[(size_t)ny * W + nx] : 0;
+                                }
+                                if (!(e && h < NP2)) continue;
+                                if (rs && h == 1) {
+                                    const int fl = min(rs, e);
+                                    e -= fl;
+                                    res[kSink * N + i] = rs - fl;
+                                }
+#pragma unroll
+                                for (int d = 0; d < 4; ++d) {
+                                    // A non-zero residue only ever points at a node
+                                    // inside the grid (graphcut.cc:18-33).
+                                    if (!rd[d] || h != hq[d] + 1) continue;
                                     const size_t q = (size_t)(y + gdy(d)) * W + x + gdx(d);
-                                    if (h != ht[q] + 1) continue;
-                                    const int fl = min(rd, e);
+                                    const int fl = min(rd[d], e);
                                     e -= fl;
                                     atomicAdd(&ex[q], fl);
-                                    res[d * N + i] = rd - fl;
-                                    res[gopp(d) * N + q] += fl;
+                                    res[d * N + i] = rd[d] - fl;
+                                    // Only this node writes its neighbour's slot
+                                    // towards it during this diagonal.
+                                    atomicAdd(&res[gopp(d) * N + q], fl);
                                     // South and east neighbours lie on the next
                                     // diagonal, which this sweep reaches later.
-                                    if (d <= 1) atomicMax(&sh.kmax, k + 1);
+                                    if (d <= 1) {
+                                        atomicMax(&sh.kmax, k + 1);
+                                        if (bits) atomicOr(&sh.diag[(k + 1) >> 5], 1u << ((k + 1) & 31));
+                                    }
                                 }
                                 ex[i] = e;
                             }
@@ -267,18 +303,31 @@ __global__ void __launch_bounds__(kThreadsAB, 1) k_alpha_beta(const AlphaBetaPar
                         // no excess, so the active diagonals bound them.
                         active_diagonals(p, sh);
                         for (int k = sh.kmin; k <= sh.kmax; ++k) {
+                            if (!diag_visit(sh, k, bits)) continue;
                             const int xlo = k - (H - 1) > 0 ? k - (H - 1) : 0;
                             const int xhi = k < W - 1 ? k : W - 1;
                             for (int x = xlo + (int)threadIdx.x; x <= xhi; x += blockDim.x) {
                                 const int y = k - x;
                                 const size_t i = (size_t)y * W + x;
-                                if (!(ex[i] && ht[i] < NP2)) continue;
-                                if (res[kSink * N + i]) {
+                                // Loaded at once: the west and north neighbours'
+                                // heights were relabelled on diagonal k - 1, the
+                                // others are untouched until later.
+                                const int e = ex[i], h = ht[i], rs = res[kSink * N + i];
+                                int rd[4], hq[4];
+#pragma unroll
+                                for (int d = 0; d < 4; ++d) {
+                                    rd[d] = res[d * N + i];
+                                    const int nx = x + gdx(d), ny = y + gdy(d);
+                                    hq[d] = (nx >= 0 && ny >= 0 && nx < W && ny < H) ? ht[(size_t)ny * W + nx] : 0;
+                                }
+                                if (!(e && h < NP2)) continue;
+                                if (rs) {
                                     ht[i] = 1;
                                 } else {
                                     int mh = NP2;
+#pragma unroll
                                     for (int d = 0; d < 4; ++d)
-                                        if (res[d * N + i]) mh = min(mh, ht[(size_t)(y + gdy(d)) * W + x + gdx(d)]);
+                                        if (rd[d]) mh = min(mh, hq[d]);
                                     ht[i] = mh + 1;
                                 }
                             }
