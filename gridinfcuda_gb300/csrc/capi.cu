@@ -23,7 +23,8 @@
 using namespace ginf_gpu;
 
 namespace ginf_gpu {
-ginf_status warmnet_forward(ginf_warmnet *n, const float *x, int nimg, int h, int w, float **y_out, cudaStream_t s);
+ginf_status warmnet_forward(ginf_warmnet *n, const float *x, int nimg, int h, int w, float **y_out, int *status,
+                            cudaStream_t s);
 int warmnet_labels(const ginf_warmnet *n);
 
 template <typename T, typename M>
@@ -1205,7 +1206,7 @@ static ginf_status decode_hbp_seeded(ginf_workspace *wsp, const ginf_grid *grid,
         }
         ++c.launches;
         if (net) {
-            if ((st = warmnet_forward(net, x, 1, lt.H, lt.W, &y, s)) != GINF_OK) break;
+            if ((st = warmnet_forward(net, x, 1, lt.H, lt.W, &y, P.status, s)) != GINF_OK) break;
             c.launches += 5;
         }
         // Seeded path: level-t messages from the prediction, its own sweeps,

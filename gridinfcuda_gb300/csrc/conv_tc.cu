@@ -1,0 +1,468 @@
+// conv_tc.cu -- the warm-start network's 3x3 convolution (the forward pass,
+// and the data gradient as a forward convolution with flipped weights) on the
+// fifth-generation tensor cores: tcgen05.mma with the accumulator in tensor
+// memory, both operands read from shared memory by matrix descriptors, the
+// input rows brought in by TMA tensor copies.
+//
+// Implicit GEMM.  A tile is M = 128 consecutive pixels of one image row,
+// N = COUT output channels, K = 9 taps x CIN input channels, BF16 operands,
+// FP32 accumulation.  Activations are NHWC BF16.  A CTA owns a strip of
+// tiles going down one 128-pixel column band of an image, so each input row
+// is loaded once (plus one halo row above and below the strip): a row
+// arrives as CIN/8 TMA copies of 130 pixels x 8 channels (the band plus one
+// pixel either side; pixels and rows outside the image read as zero, which
+// is the convolution's zero padding), landing in the canonical K-major
+// layout without swizzle: per 8-channel chunk a slab of 130 pixel rows of
+// 16 bytes (slabs 2176 bytes apart, so that each copy starts 128-byte
+// aligned).  Eight consecutive pixels of a slab are one 8x16-byte core
+// matrix, so the A operand of tap (dy, dx) is the slab of row y + dy read
+// from pixel dx + 1 on -- the nine taps are nine descriptors over three row
+// buffers, nothing is copied per tap.  The weights, [tap][chunk][co][8] in
+// the same layout, stay in shared memory for the CTA's life.
+//
+// Roles (192 threads): warp 4 lane 0 issues the row copies into a ring of
+// RING buffers; warp 5 lane 0 issues the 9 * CIN / 16 MMAs of a tile into one
+// of two tensor-memory accumulators and commits them to mbarriers (the
+// accumulator is full, and a row buffer whose last tile is done is free);
+// warps 0-3 read the accumulator back (warp w owns lanes 32w..32w+31, i.e.
+// pixels 32w.. of the tile), add the bias, apply ReLU and the residual, and
+// store.  Every wait is bounded (DEV_ERR_TIMEOUT in the status word), and
+// the tensor memory is released on every path.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "ginf_internal.h"
+#include "ptx.cuh"
+
+namespace ginf_gpu {
+
+struct ConvTcParams {
+    const __nv_bfloat16 *wt;  // [COUT][9][CIN], tap = (dy + 1) * 3 + dx + 1
+    const float *bias;       // COUT, or null
+    const float *res;        // FP32 residual [pixel][COUT] added after the activation, or null
+    void *out;               // [pixel][COUT], FP32 or BF16
+    int n, h, w;             // images, rows, columns
+    int bands, chunks, rows_per_chunk, items;
+    int *status;
+};
+
+namespace {
+
+constexpr int kTileM = 128;            // pixels per tile (MMA M)
+constexpr int kSlab = kTileM + 2;      // pixels per row copy: the band and one either side
+constexpr int kPitch = 136 * 16;       // bytes between chunk slabs (a copy's destination is 128-byte aligned)
+constexpr int kThreadsTc = 192;        // warps 0-3 epilogue, 4 copies, 5 MMA
+constexpr int kCopyWarp = 4, kMmaWarp = 5;
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// One box of the 5-D row map (8 channels, chunk, x, row, image).
+__device__ __forceinline__ void tma_load_row(uint32_t dst, const CUtensorMap *map, int chunk, int x, int row, int img,
+                                             uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+        "%6}], [%7];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(chunk), "r"(x), "r"(row), "r"(img), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// Shared-memory matrix descriptor, canonical layout without swizzle: start
+// address, leading byte offset (between core matrices adjacent in K), stride
+// byte offset (between core matrices adjacent in M or N), version 1.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t instr_desc_bf16(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTileM >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+// Arrives on bar once every tcgen05 operation this thread issued before is done.
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this warp's 32 lanes (one lane per thread),
+// waited for before returning.
+__device__ __forceinline__ void tmem_load16(uint32_t taddr, float *v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct Item {
+    int img, x0, y0, rows;
+};
+
+// Work item: (image, 128-pixel band, chunk of rows_per_chunk rows), chunks
+// of one band adjacent so that neighbouring CTAs share halo rows in L2.
+__device__ __forceinline__ Item item_of(const ConvTcParams &p, int it) {
+    Item r;
+    const int chunk = it % p.chunks, rest = it / p.chunks;
+    r.x0 = (rest % p.bands) * kTileM;
+    r.img = rest / p.bands;
+    r.y0 = chunk * p.rows_per_chunk;
+    r.rows = min(p.rows_per_chunk, p.h - r.y0);
+    return r;
+}
+
+template <int CIN, int COUT, bool OUT_F32, int RING>
+struct TcLayout {
+    static constexpr int kChunks = CIN / 8;
+    static constexpr int kRowBytes = kChunks * kPitch;      // one row buffer: [chunk][130 pixels + pad][16 B]
+    static constexpr int kCopyBytes = kChunks * kSlab * 16;  // what one row's copies write
+    static constexpr int kWBytes = 9 * CIN * COUT * 2;      // [tap][chunk][co][16 B]
+    static constexpr int kRows = 0;
+    static constexpr int kW = kRows + RING * kRowBytes;
+    static constexpr int kBias = kW + kWBytes;
+    static constexpr int kOutBytes = COUT * (OUT_F32 ? 4 : 2);  // one pixel's outputs
+    static constexpr int kChunksOut = kOutBytes / 16;
+    static constexpr int kStagePitch = kOutBytes + 16;
+    static constexpr int kStage = (kBias + COUT * 4 + 15) / 16 * 16;  // 4 warps x 32 pixel rows
+    static constexpr int kBars = kStage + 4 * 32 * kStagePitch;
+    static constexpr int kNumBars = 2 * RING + 5;  // full[RING], empty[RING], acc_full[2], acc_empty[2], done
+    static constexpr int kTmemSlot = kBars + kNumBars * 8;
+    static constexpr int kAbort = kTmemSlot + 4;
+    static constexpr int kBytes = kAbort + 4;
+    static constexpr uint32_t kCols = 2 * COUT < 32 ? 32 : 2 * COUT;  // two accumulators, a power of two >= 32
+};
+
+template <int CIN, int COUT, bool RELU, bool OUT_F32, int RING>
+__global__ void __launch_bounds__(kThreadsTc, 1)
+    k_conv_tc(const __grid_constant__ CUtensorMap rows_map, const ConvTcParams p) {
+    using Lay = TcLayout<CIN, COUT, OUT_F32, RING>;
+    static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 256, "tile shape");
+    extern __shared__ __align__(1024) unsigned char sm[];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sm + Lay::kBars);
+    uint64_t *full = bars, *empty = bars + RING, *acc_full = bars + 2 * RING, *acc_empty = acc_full + 2,
+             *done = acc_empty + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + Lay::kTmemSlot);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(sm + Lay::kAbort);
+    float *bias = reinterpret_cast<float *>(sm + Lay::kBias);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char *stage = sm + Lay::kStage + (warp & 3) * 32 * Lay::kStagePitch;
+
+    // Weights into [tap][chunk][co][8 channels], the bias (zero without one).
+    for (int e = threadIdx.x; e < 9 * Lay::kChunks * COUT; e += blockDim.x) {
+        const int co = e % COUT, t = e / COUT, c8 = t % Lay::kChunks, tap = t / Lay::kChunks;
+        *reinterpret_cast<uint4 *>(sm + Lay::kW + (size_t)e * 16) =
+            *reinterpret_cast<const uint4 *>(p.wt + ((size_t)co * 9 + tap) * CIN + c8 * 8);
+    }
+    for (int c = threadIdx.x; c < COUT; c += blockDim.x) bias[c] = p.bias ? p.bias[c] : 0.f;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < RING; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&acc_full[i], 1);
+            mbar_init(&acc_empty[i], 4 * 32);
+        }
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        fence_barrier_init();
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                     "r"(Lay::kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_proxy_async_shared();  // the weights, written by threads, are read by the tensor cores
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    if (smem_addr(sm) & 127u) {  // row copies need 128-byte aligned destinations
+        if (threadIdx.x == 0 && p.status) atomicOr(p.status, DEV_ERR_BOUNDS);
+        *abort_flag = 1;
+    }
+    __syncthreads();
+
+    if (warp == kCopyWarp) {
+        if (lane == 0) {
+            uint32_t ld = 0;
+            for (int it = blockIdx.x; it < p.items && !*abort_flag; it += gridDim.x) {
+                const Item t = item_of(p, it);
+                for (int r = t.y0 - 1; r <= t.y0 + t.rows; ++r, ++ld) {
+                    const int slot = (int)(ld % RING);
+                    if (!mbar_wait_bounded(&empty[slot], ((ld / RING) & 1u) ^ 1u, p.status)) {
+                        *abort_flag = 1;
+                        break;
+                    }
+                    mbar_arrive_expect_tx(&full[slot], Lay::kCopyBytes);
+                    const uint32_t dst = smem_addr(sm + Lay::kRows + slot * Lay::kRowBytes);
+#pragma unroll
+                    for (int c = 0; c < Lay::kChunks; ++c)
+                        tma_load_row(dst + c * kPitch, &rows_map, c, t.x0 - 1, r, t.img, &full[slot]);
+                }
+            }
+            // Copies still in flight land before the CTA's shared memory goes.
+            for (uint32_t q = ld > RING ? ld - RING : 0; q < ld; ++q)
+                mbar_wait_bounded(&full[q % RING], (q / RING) & 1u, nullptr);
+        }
+        __syncwarp();
+    } else if (warp == kMmaWarp) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = instr_desc_bf16(COUT);
+            const uint32_t wbase = smem_addr(sm + Lay::kW), rbase = smem_addr(sm + Lay::kRows);
+            uint32_t ld = 0, tile = 0;
+            bool ok = true;
+            for (int it = blockIdx.x; it < p.items && ok && !*abort_flag; it += gridDim.x) {
+                const Item t = item_of(p, it);
+                const uint32_t base = ld;
+                for (int j = 0; j < t.rows && ok; ++j, ++tile) {
+                    // Rows y - 1, y, y + 1 of output row y = y0 + j are copies base + j .. base + j + 2.
+                    for (uint32_t q = j == 0 ? base : base + j + 2; q <= base + j + 2 && ok; ++q)
+                        ok = mbar_wait_bounded(&full[q % RING], (q / RING) & 1u, p.status);
+                    const uint32_t acc = tile & 1u;
+                    if (ok) ok = mbar_wait_bounded(&acc_empty[acc], ((tile >> 1) & 1u) ^ 1u, p.status);
+                    if (!ok) break;
+                    tc_fence_after();
+                    const uint32_t d = tmem + acc * COUT;
+                    uint32_t accumulate = 0;
+#pragma unroll
+                    for (int dy = 0; dy < 3; ++dy) {
+                        const uint32_t row = rbase + ((base + j + dy) % RING) * Lay::kRowBytes;
+#pragma unroll
+                        for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+                            for (int ks = 0; ks < CIN / 16; ++ks) {
+                                const uint64_t a = smem_desc(row + 2 * ks * kPitch + dx * 16, kPitch, 128);
+                                const uint64_t b =
+                                    smem_desc(wbase + (((dy * 3 + dx) * Lay::kChunks + 2 * ks) * COUT) * 16, COUT * 16, 128);
+                                umma_bf16(d, a, b, idesc, accumulate);
+                                accumulate = 1;
+                            }
+                    }
+                    umma_commit(&acc_full[acc]);
+                    // Copy base + j (row y - 1) has had its last tile; after the
+                    // strip's last tile so have the two below it.
+                    umma_commit(&empty[(base + j) % RING]);
+                    if (j == t.rows - 1) {
+                        umma_commit(&empty[(base + j + 1) % RING]);
+                        umma_commit(&empty[(base + j + 2) % RING]);
+                    }
+                }
+                ld = base + t.rows + 2;
+            }
+            if (!ok) *abort_flag = 1;
+            umma_commit(done);
+            mbar_wait_bounded(done, 0, nullptr);
+        }
+        __syncwarp();
+    } else {
+        // Epilogue: warp w reads lanes 32w..32w+31 of the accumulator.
+        uint32_t tile = 0;
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        // The tensor-memory loads are warp-collective: every decision to stop
+        // is taken by the whole warp.
+        for (int it = blockIdx.x; it < p.items && !__any_sync(~0u, *abort_flag); it += gridDim.x) {
+            const Item t = item_of(p, it);
+            for (int j = 0; j < t.rows; ++j, ++tile) {
+                const uint32_t acc = tile & 1u;
+                if (!__all_sync(~0u, mbar_wait_bounded(&acc_full[acc], (tile >> 1) & 1u, p.status))) {
+                    *abort_flag = 1;
+                    break;
+                }
+                tc_fence_after();
+                float v[COUT];
+#pragma unroll
+                for (int c = 0; c < COUT; c += 16) tmem_load16(tmem + lane_base + acc * COUT + c, v + c);
+                tc_fence_before();
+                mbar_arrive(&acc_empty[acc]);
+#pragma unroll
+                for (int c = 0; c < COUT; ++c) {
+                    v[c] += bias[c];
+                    if (RELU) v[c] = fmaxf(v[c], 0.f);
+                }
+                // This lane's pixel into the warp's staging rows (a pitch of
+                // one 16-byte chunk more than a pixel's outputs keeps eight
+                // consecutive lanes on distinct banks) ...
+                unsigned char *row = stage + lane * Lay::kStagePitch;
+#pragma unroll
+                for (int c = 0; c < Lay::kChunksOut; ++c) {
+                    uint4 q;
+                    if (OUT_F32) {
+                        q = make_uint4(__float_as_uint(v[4 * c]), __float_as_uint(v[4 * c + 1]),
+                                       __float_as_uint(v[4 * c + 2]), __float_as_uint(v[4 * c + 3]));
+                    } else {
+                        uint32_t w4[4];
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            w4[k] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[8 * c + 2 * k])) |
+                                    ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[8 * c + 2 * k + 1])) << 16);
+                        q = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+                    }
+                    *reinterpret_cast<uint4 *>(row + c * 16) = q;
+                }
+                __syncwarp();
+                // ... then the warp's 32 pixels, contiguous in the output,
+                // written 512 bytes per instruction (the residual read the
+                // same way).
+                const int x = t.x0 + warp * 32;
+                const int valid = p.w - x < 32 ? p.w - x : 32;
+                const size_t pix = ((size_t)t.img * p.h + t.y0 + j) * p.w + x;
+                uint4 *o = reinterpret_cast<uint4 *>(static_cast<unsigned char *>(p.out) + pix * Lay::kOutBytes);
+                const uint4 *rs = OUT_F32 && p.res ? reinterpret_cast<const uint4 *>(p.res + pix * COUT) : nullptr;
+                const int nq = valid * Lay::kChunksOut;
+                uint4 r[Lay::kChunksOut];  // all residual loads in flight before the first store
+                if (OUT_F32 && rs) {
+#pragma unroll
+                    for (int i = 0; i < Lay::kChunksOut; ++i)
+                        if (lane + 32 * i < nq) r[i] = rs[lane + 32 * i];
+                }
+#pragma unroll
+                for (int i = 0; i < Lay::kChunksOut; ++i) {
+                    const int q = lane + 32 * i;
+                    if (q >= nq) break;
+                    uint4 val = *reinterpret_cast<const uint4 *>(stage + (q / Lay::kChunksOut) * Lay::kStagePitch +
+                                                                 (q % Lay::kChunksOut) * 16);
+                    if (OUT_F32 && rs)
+                        val = make_uint4(__float_as_uint(__uint_as_float(val.x) + __uint_as_float(r[i].x)),
+                                         __float_as_uint(__uint_as_float(val.y) + __uint_as_float(r[i].y)),
+                                         __float_as_uint(__uint_as_float(val.z) + __uint_as_float(r[i].z)),
+                                         __float_as_uint(__uint_as_float(val.w) + __uint_as_float(r[i].w)));
+                    o[q] = val;
+                }
+                __syncwarp();
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Lay::kCols) : "memory");
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+        cudaGetLastError();
+    });
+    return fn;
+}
+
+template <int CIN, int COUT, bool RELU, bool OUT_F32>
+cudaError_t launch_conv_tc(const __nv_bfloat16 *in, ConvTcParams p, cudaStream_t s) {
+    // The deepest ring of row buffers (3 to 8) that leaves room for two CTAs
+    // per SM (228 KB of shared memory, 1 KB of it reserved per CTA).
+    constexpr int kBudget = 113 * 1024;
+    constexpr int kFixed = TcLayout<CIN, COUT, OUT_F32, 8>::kBytes - 8 * TcLayout<CIN, COUT, OUT_F32, 8>::kRowBytes;
+    constexpr int kFit = (kBudget - kFixed) / TcLayout<CIN, COUT, OUT_F32, 8>::kRowBytes;
+    constexpr int RING = kFit < 3 ? 3 : (kFit > 8 ? 8 : kFit);
+    using Lay = TcLayout<CIN, COUT, OUT_F32, RING>;
+    auto kern = k_conv_tc<CIN, COUT, RELU, OUT_F32, RING>;
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [&] {
+        attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::kBytes);
+    });
+    if (attr_err != cudaSuccess) return attr_err;
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode) return cudaErrorNotSupported;
+    // Rows map over the NHWC input: (8 channels, chunk, x, row, image), packed strides.
+    alignas(64) CUtensorMap map;
+    const cuuint64_t dims[5] = {8, (cuuint64_t)(CIN / 8), (cuuint64_t)p.w, (cuuint64_t)p.h, (cuuint64_t)p.n};
+    const cuuint64_t strides[4] = {16, (cuuint64_t)CIN * 2, (cuuint64_t)p.w * CIN * 2, (cuuint64_t)p.h * p.w * CIN * 2};
+    const cuuint32_t box[5] = {8, 1, kSlab, 1, 1};
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    if (encode(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<__nv_bfloat16 *>(in), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreadsTc, Lay::kBytes)) != cudaSuccess)
+        return e;
+    const int slots = sms * (per_sm > 0 ? per_sm : 1);
+    // Split each band's rows into chunks so that the items about fill the GPU
+    // once, keeping at least four rows per chunk (two halo rows per chunk).
+    p.bands = (p.w + kTileM - 1) / kTileM;
+    const long long strips = (long long)p.n * p.bands;
+    long long rpc = (strips * p.h + slots - 1) / slots;
+    if (rpc < 4) rpc = 4;
+    if (rpc > p.h) rpc = p.h;
+    p.rows_per_chunk = (int)rpc;
+    p.chunks = (p.h + p.rows_per_chunk - 1) / p.rows_per_chunk;
+    const long long items = strips * p.chunks;
+    if (items > 0x7fffffffLL) return cudaErrorInvalidValue;
+    p.items = (int)items;
+    const int grid = p.items < slots ? p.items : slots;
+    kern<<<grid, kThreadsTc, Lay::kBytes, s>>>(map, p);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// 3x3 convolution of NHWC BF16 input with weights [COUT][9][CIN] on the
+// tcgen05 path; cudaErrorInvalidValue for a channel pair it is not built for.
+cudaError_t conv_fwd_tc(int cin, int cout, bool relu, bool out_f32, const __nv_bfloat16 *in, const __nv_bfloat16 *w,
+                        const float *bias, int nimg, int h, int wd, void *out, const float *res, int *status,
+                        cudaStream_t s) {
+    if (((uintptr_t)in | (uintptr_t)w | (uintptr_t)out | (uintptr_t)res) & 15) return cudaErrorMisalignedAddress;
+    ConvTcParams p{};
+    p.wt = w;
+    p.bias = bias;
+    p.res = res;
+    p.out = out;
+    p.n = nimg;
+    p.h = h;
+    p.w = wd;
+    p.status = status;
+#define GINF_TC_CASE(CI, CO)                                                                    \
+    if (cin == CI && cout == CO) {                                                              \
+        if (out_f32) return relu ? cudaErrorInvalidValue : launch_conv_tc<CI, CO, false, true>(in, p, s); \
+        return relu ? launch_conv_tc<CI, CO, true, false>(in, p, s)                             \
+                    : launch_conv_tc<CI, CO, false, false>(in, p, s);                           \
+    }
+    GINF_TC_CASE(16, 32)
+    GINF_TC_CASE(32, 32)
+    GINF_TC_CASE(64, 32)
+    GINF_TC_CASE(32, 16)
+    GINF_TC_CASE(32, 64)
+#undef GINF_TC_CASE
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace ginf_gpu

@@ -1,9 +1,10 @@
 // warmnet.cu -- the learned warm start: a small convolutional network that
 // maps the costs of a pyramid level to the messages its nodes should start
 // from (on the beliefs' scale), with
-// hand-written tensor-core (mma.sync m16n8k16 BF16, FP32 accumulate)
-// forward, data-gradient and weight-gradient kernels, the loss, ReLU,
-// bias-gradient and Adam kernels, and a checkpoint format.
+// hand-written tensor-core kernels -- the forward and data-gradient
+// convolutions on tcgen05 with tensor-memory accumulators (conv_tc.cu), the
+// weight gradient on mma.sync m16n8k16 (BF16, FP32 accumulate) -- the loss,
+// ReLU, bias-gradient and Adam kernels, and a checkpoint format.
 //
 // Network (L labels, h hidden channels): conv3x3(L->h) ReLU, conv3x3(h->h)
 // ReLU, conv3x3(h->h) ReLU, conv3x3(h->L); zero padding; activations NHWC.
@@ -26,6 +27,11 @@
 #include "ginf_internal.h"
 
 namespace ginf_gpu {
+
+cudaError_t conv_fwd_tc(int cin, int cout, bool relu, bool out_f32, const __nv_bfloat16 *in, const __nv_bfloat16 *w,
+                        const float *bias, int nimg, int h, int wd, void *out, const float *res, int *status,
+                        cudaStream_t s);
+
 namespace {
 
 constexpr int kThreads = 256;
@@ -47,85 +53,6 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
 struct Geo {
     int n, h, w;  // images, rows, columns
 };
-
-// Pair of input channels (c, c+1) at the pixel shifted by (dy, dx), zero
-// outside the image.
-__device__ __forceinline__ uint32_t load_pair(const __nv_bfloat16 *in, int cin, Geo g, int pix, int dy, int dx,
-                                              int c) {
-    const int x = pix % g.w, t = pix / g.w, y = t % g.h, n = t / g.h;
-    const int yy = y + dy, xx = x + dx;
-    if (pix < 0 || yy < 0 || yy >= g.h || xx < 0 || xx >= g.w) return 0u;
-    return *reinterpret_cast<const uint32_t *>(in + ((size_t)(n * g.h + yy) * g.w + xx) * cin + c);
-}
-
-// Forward 3x3 convolution as an implicit GEMM: M = pixels, N = COUT,
-// K = 9*CIN.  A warp owns 16 consecutive pixels and all COUT outputs; each
-// mma consumes one 16-channel slice of one tap.  Weights w[co][tap][ci].
-// RELU applies max(0, .); OUT_F32 writes FP32 (else BF16).  With RES the
-// FP32 output is res + conv (the residual of the last layer).
-template <int CIN, int COUT, bool RELU, bool OUT_F32, bool BIAS>
-__global__ void __launch_bounds__(128) k_conv_fwd(const __nv_bfloat16 *__restrict__ in, const __nv_bfloat16 *__restrict__ w,
-                                                  const float *__restrict__ bias, Geo g, void *out,
-                                                  const float *__restrict__ res) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int gid = lane >> 2, tig = lane & 3;
-    const int npix = g.n * g.h * g.w;
-    const int p0 = (blockIdx.x * 4 + warp) * 16;
-    if (p0 >= npix) return;
-    const int pa = p0 + gid, pb = p0 + gid + 8;
-    float acc[COUT / 8][4];
-#pragma unroll
-    for (int j = 0; j < COUT / 8; ++j)
-#pragma unroll
-        for (int e = 0; e < 4; ++e) acc[j][e] = 0.f;
-#pragma unroll 1
-    for (int tap = 0; tap < 9; ++tap) {
-        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-#pragma unroll
-        for (int c0 = 0; c0 < CIN; c0 += 16) {
-            uint32_t a[4];
-            const int c = c0 + tig * 2;
-            a[0] = load_pair(in, CIN, g, pa < npix ? pa : -1, dy, dx, c);
-            a[1] = load_pair(in, CIN, g, pb < npix ? pb : -1, dy, dx, c);
-            a[2] = load_pair(in, CIN, g, pa < npix ? pa : -1, dy, dx, c + 8);
-            a[3] = load_pair(in, CIN, g, pb < npix ? pb : -1, dy, dx, c + 8);
-            const int k = tap * CIN + c;
-#pragma unroll
-            for (int j = 0; j < COUT / 8; ++j) {
-                const __nv_bfloat16 *wr = w + (size_t)(j * 8 + gid) * 9 * CIN + k;
-                uint32_t b[2];
-                b[0] = *reinterpret_cast<const uint32_t *>(wr);
-                b[1] = *reinterpret_cast<const uint32_t *>(wr + 8);
-                mma_bf16(acc[j], a, b);
-            }
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < COUT / 8; ++j) {
-        const int co = j * 8 + tig * 2;
-        const float b0 = BIAS ? bias[co] : 0.f, b1 = BIAS ? bias[co + 1] : 0.f;
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            const int p = half ? pb : pa;
-            if (p >= npix) continue;
-            float v0 = acc[j][2 * half] + b0, v1 = acc[j][2 * half + 1] + b1;
-            if (RELU) {
-                v0 = fmaxf(v0, 0.f);
-                v1 = fmaxf(v1, 0.f);
-            }
-            if (OUT_F32) {
-                if (res) {
-                    v0 += res[(size_t)p * COUT + co];
-                    v1 += res[(size_t)p * COUT + co + 1];
-                }
-                *reinterpret_cast<float2 *>(static_cast<float *>(out) + (size_t)p * COUT + co) = make_float2(v0, v1);
-            } else {
-                *reinterpret_cast<uint32_t *>(static_cast<__nv_bfloat16 *>(out) + (size_t)p * COUT + co) =
-                    pack_bf16(__float2bfloat16_rn(v0), __float2bfloat16_rn(v1));
-            }
-        }
-    }
-}
 
 // Weight gradient: dW[co][tap][ci] = sum over pixels of dout[p][co] *
 // in[p shifted by tap][ci], as GEMM M = COUT, N = 9*CIN, K = pixels.  Block
@@ -288,18 +215,8 @@ uint64_t fnv1a(const void *data, size_t n, uint64_t h = 1469598103934665603ull) 
 
 }  // namespace
 
-// Conv kernel instantiations for the channel counts the network uses
+// Weight-gradient instantiations for the channel counts the network uses
 // (L in {16, 32, 64}, 32 hidden channels).
-template <int CIN, int COUT, bool RELU, bool OUT_F32>
-cudaError_t conv_fwd_t(const __nv_bfloat16 *in, const __nv_bfloat16 *w, const float *bias, Geo g, void *out,
-                       const float *res, cudaStream_t s) {
-    const int npix = g.n * g.h * g.w;
-    const unsigned blocks = (unsigned)((npix + 63) / 64);
-    if (bias) k_conv_fwd<CIN, COUT, RELU, OUT_F32, true><<<blocks, 128, 0, s>>>(in, w, bias, g, out, res);
-    else k_conv_fwd<CIN, COUT, RELU, OUT_F32, false><<<blocks, 128, 0, s>>>(in, w, bias, g, out, res);
-    return cudaGetLastError();
-}
-
 template <int CIN, int COUT>
 cudaError_t conv_wgrad_t(const __nv_bfloat16 *dout, const __nv_bfloat16 *in, Geo g, float *partials, float *dw,
                          cudaStream_t s) {
@@ -343,6 +260,7 @@ struct ginf_warmnet {
     size_t cap_partials = 0;
     double *loss_part = nullptr;
     float *loss_dev = nullptr;
+    int *status = nullptr;  // device word: DEV_ERR_* from the convolution kernels' bounded waits
 };
 
 namespace {
@@ -389,7 +307,18 @@ ginf_status alloc_params(ginf_warmnet *n) {
     GINF_WCK(cudaMalloc(&n->wflip, wf * sizeof(__nv_bfloat16)));
     GINF_WCK(cudaMalloc(&n->loss_part, 1024 * sizeof(double)));
     GINF_WCK(cudaMalloc(&n->loss_dev, sizeof(float)));
+    GINF_WCK(cudaMalloc(&n->status, sizeof(int)));
+    GINF_WCK(cudaMemset(n->status, 0, sizeof(int)));
     return GINF_OK;
+}
+
+// After a synchronisation: a wait in a convolution kernel that ran out.
+ginf_status check_status(ginf_warmnet *n) {
+    int st = 0;
+    GINF_WCK(cudaMemcpy(&st, n->status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st == 0) return GINF_OK;
+    GINF_WCK(cudaMemset(n->status, 0, sizeof(int)));
+    return wfail(GINF_ERR_TIMEOUT, "warm-start convolution: a device wait ran out (status " + std::to_string(st) + ")");
 }
 
 ginf_status refresh_bf16(ginf_warmnet *n, cudaStream_t s) {
@@ -429,22 +358,10 @@ ginf_status ensure_batch(ginf_warmnet *n, size_t pix) {
     return GINF_OK;
 }
 
-// conv dispatch by (cin, cout) for the supported shapes
+// 3x3 convolution on the tcgen05 path for the supported (cin, cout) pairs.
 cudaError_t conv_fwd(int cin, int cout, bool relu, bool out_f32, const __nv_bfloat16 *in, const __nv_bfloat16 *w,
-                     const float *bias, Geo g, void *out, const float *res, cudaStream_t s) {
-#define GINF_CONV_CASE(CI, CO)                                                                         \
-    if (cin == CI && cout == CO) {                                                                     \
-        if (out_f32) return conv_fwd_t<CI, CO, false, true>(in, w, bias, g, out, res, s);             \
-        if (relu) return conv_fwd_t<CI, CO, true, false>(in, w, bias, g, out, res, s);                \
-        return conv_fwd_t<CI, CO, false, false>(in, w, bias, g, out, res, s);                         \
-    }
-    GINF_CONV_CASE(16, 32)
-    GINF_CONV_CASE(32, 32)
-    GINF_CONV_CASE(64, 32)
-    GINF_CONV_CASE(32, 16)
-    GINF_CONV_CASE(32, 64)
-#undef GINF_CONV_CASE
-    return cudaErrorInvalidValue;
+                     const float *bias, Geo g, void *out, const float *res, int *status, cudaStream_t s) {
+    return conv_fwd_tc(cin, cout, relu, out_f32, in, w, bias, g.n, g.h, g.w, out, res, status, s);
 }
 
 cudaError_t conv_wgrad(int cin, int cout, const __nv_bfloat16 *dout, const __nv_bfloat16 *in, Geo g, float *part,
@@ -460,7 +377,7 @@ cudaError_t conv_wgrad(int cin, int cout, const __nv_bfloat16 *dout, const __nv_
     return cudaErrorInvalidValue;
 }
 
-ginf_status forward(ginf_warmnet *n, const float *x, Geo g, cudaStream_t s) {
+ginf_status forward(ginf_warmnet *n, const float *x, Geo g, int *status, cudaStream_t s) {
     const size_t pix = (size_t)g.n * g.h * g.w;
     ginf_status st = ensure_batch(n, pix);
     if (st != GINF_OK) return st;
@@ -469,9 +386,9 @@ ginf_status forward(ginf_warmnet *n, const float *x, Geo g, cudaStream_t s) {
     GINF_WCK(cudaGetLastError());
     for (int l = 0; l < 3; ++l)
         GINF_WCK(conv_fwd(n->cin[l], n->cout[l], true, false, n->a[l], n->wbf + n->woff[l], n->params + n->boff[l], g,
-                          n->a[l + 1], nullptr, s));
+                          n->a[l + 1], nullptr, status, s));
     GINF_WCK(conv_fwd(n->cin[3], n->cout[3], false, true, n->a[3], n->wbf + n->woff[3], n->params + n->boff[3], g,
-                      n->y, n->x32, s));
+                      n->y, n->x32, status, s));
     return GINF_OK;
 }
 
@@ -500,7 +417,7 @@ ginf_status backward(ginf_warmnet *n, const float *target, Geo g, cudaStream_t s
         // data gradient: conv of the (BF16) output gradient with the flipped weights
         k_flip_weights<<<nblocks((size_t)ci * 9 * co), kThreads, 0, s>>>(n->wbf + n->woff[l], ci, co, n->wflip);
         GINF_WCK(cudaGetLastError());
-        GINF_WCK(conv_fwd(co, ci, false, true, n->gb, n->wflip, nullptr, g, n->gtmp, nullptr, s));
+        GINF_WCK(conv_fwd(co, ci, false, true, n->gb, n->wflip, nullptr, g, n->gtmp, nullptr, n->status, s));
         // through the ReLU of layer l-1's output
         k_relu_bwd<<<nblocks(pix * ci), kThreads, 0, s>>>(n->gtmp, n->a[l], pix * ci, n->g32, n->gb);
         GINF_WCK(cudaGetLastError());
@@ -527,11 +444,14 @@ constexpr uint32_t kVersion = 1;
 
 namespace ginf_gpu {
 // Used by the learned HBP solve in capi.cu: forward pass on level-t inputs.
-ginf_status warmnet_forward(ginf_warmnet *n, const float *x, int nimg, int h, int w, float **y_out, cudaStream_t s) {
+// Device waits that run out are recorded in `status` (the network's own
+// word when null).
+ginf_status warmnet_forward(ginf_warmnet *n, const float *x, int nimg, int h, int w, float **y_out, int *status,
+                            cudaStream_t s) {
     ginf_status st = check_geo(n, nimg, h, w);
     if (st != GINF_OK) return st;
     Geo g{nimg, h, w};
-    st = forward(n, x, g, s);
+    st = forward(n, x, g, status ? status : n->status, s);
     if (st != GINF_OK) return st;
     *y_out = n->y;
     return GINF_OK;
@@ -594,6 +514,7 @@ ginf_status ginf_warmnet_destroy(ginf_warmnet *n) {
     cudaFree(n->partials);
     cudaFree(n->loss_part);
     cudaFree(n->loss_dev);
+    cudaFree(n->status);
     delete n;
     return GINF_OK;
 }
@@ -624,11 +545,11 @@ ginf_status ginf_warmnet_forward(ginf_warmnet *n, const float *x, int32_t nimg, 
     ginf_gpu::set_last_error("");
     float *y = nullptr;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    ginf_status st = warmnet_forward(n, x, nimg, h, w, &y, s);
+    ginf_status st = warmnet_forward(n, x, nimg, h, w, &y, nullptr, s);
     if (st != GINF_OK) return st;
     GINF_WCK(cudaMemcpyAsync(out, y, (size_t)nimg * h * w * n->L * sizeof(float), cudaMemcpyDeviceToDevice, s));
     GINF_WCK(cudaStreamSynchronize(s));
-    return GINF_OK;
+    return check_status(n);
 }
 
 ginf_status ginf_warmnet_gradients(ginf_warmnet *n, const float *x, const float *target, int32_t nimg, int32_t h,
@@ -638,13 +559,13 @@ ginf_status ginf_warmnet_gradients(ginf_warmnet *n, const float *x, const float 
     if (st != GINF_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     Geo g{nimg, h, w};
-    if ((st = forward(n, x, g, s)) != GINF_OK) return st;
+    if ((st = forward(n, x, g, n->status, s)) != GINF_OK) return st;
     if ((st = backward(n, target, g, s)) != GINF_OK) return st;
     if (loss) GINF_WCK(cudaMemcpyAsync(loss, n->loss_dev, sizeof(float), cudaMemcpyDeviceToHost, s));
     if (grads_host)
         GINF_WCK(cudaMemcpyAsync(grads_host, n->grads, n->nparams * sizeof(float), cudaMemcpyDeviceToHost, s));
     GINF_WCK(cudaStreamSynchronize(s));
-    return GINF_OK;
+    return check_status(n);
 }
 
 ginf_status ginf_warmnet_train_step(ginf_warmnet *n, const float *x, const float *target, int32_t nimg, int32_t h,
@@ -654,7 +575,7 @@ ginf_status ginf_warmnet_train_step(ginf_warmnet *n, const float *x, const float
     if (st != GINF_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     Geo g{nimg, h, w};
-    if ((st = forward(n, x, g, s)) != GINF_OK) return st;
+    if ((st = forward(n, x, g, n->status, s)) != GINF_OK) return st;
     if ((st = backward(n, target, g, s)) != GINF_OK) return st;
     n->step += 1;
     const float b1 = 0.9f, b2 = 0.999f;
@@ -664,7 +585,7 @@ ginf_status ginf_warmnet_train_step(ginf_warmnet *n, const float *x, const float
     GINF_WCK(cudaGetLastError());
     if (loss) GINF_WCK(cudaMemcpyAsync(loss, n->loss_dev, sizeof(float), cudaMemcpyDeviceToHost, s));
     GINF_WCK(cudaStreamSynchronize(s));
-    return GINF_OK;
+    return check_status(n);
 }
 
 // Checkpoint: magic "GINFWNET", u32 version, u32 L, u32 hidden, i64 Adam step,
