@@ -50,6 +50,7 @@ WORKLOADS = {
     "batch": dict(name="batch64_lbp_200x150-1280x720_L16-64_30it", W=0, H=0, L=0, levels=1, iters=30, icm=0,
                   count=64),
     "alphabeta": dict(name="alpha_beta_384x288_L16_int_1pass", W=384, H=288, L=16, levels=1, iters=1, icm=0),
+    "warmnet": dict(name="warmnet_forward_960x540_L64", W=960, H=540, L=64, levels=1, iters=0, icm=0),
 }
 METRIC = "node-label-iters/s (LBP)"
 UNIT = "node*label*iter/s"
@@ -824,6 +825,90 @@ def run_alphabeta(args, cfg):
     ws.close()
 
 
+# ---------------------------------------------------------------- warm-start network
+
+def warmnet_bytes_flops(W, H, L, hidden=32):
+    """Algorithmic HBM bytes and FLOPs of one forward pass over an n=1, HxW,
+    L-label input: the FP32 -> BF16 conversion of x, four 3x3 convolutions
+    (BF16 activations, each read once and written once), the last layer's
+    FP32 residual read and FP32 output write."""
+    pix = W * H
+    ch = [L, hidden, hidden, hidden, L]
+    nbytes = pix * L * (4 + 2)                      # x read as FP32, written as BF16
+    for i in range(4):
+        nbytes += pix * ch[i] * 2                   # layer input (BF16)
+        nbytes += pix * ch[i + 1] * (4 if i == 3 else 2)
+    nbytes += pix * L * 4                           # residual (x, FP32)
+    flops = 2 * pix * 9 * sum(ch[i] * ch[i + 1] for i in range(4))
+    return nbytes, flops
+
+
+def run_warmnet(args, cfg):
+    """The warm-start network's forward pass (x = level costs, y = x +
+    net(x)) on a 960x540x64 input -- level 1 of a 1920x1080x64 grid -- through
+    the C ABI (ginf_warmnet_forward, device buffers), its four 3x3
+    convolutions on tcgen05 with tensor-memory accumulators; and one training
+    step (forward, loss, data and weight gradients, Adam) on a batch of 16
+    level-1 inputs of 512x384 grids.  Each call synchronises, so a step's
+    time includes the host's return; the per-kernel split is the ncu launch
+    list's."""
+    import torch
+    from gridinfcuda_gb300 import capi
+    torch.cuda.set_device(0)
+    W, H, L = cfg["W"], cfg["H"], cfg["L"]
+    net = capi.WarmNet(num_labels=L, hidden=32, seed=1)
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.rand((1, H, W, L), device="cuda", generator=gen) * 4
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        y = net.forward(x, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for a, b in evs:
+        a.record(stream)
+        y = net.forward(x, stream=stream.cuda_stream)
+        b.record(stream)
+    torch.cuda.synchronize()
+    ms = sorted(a.elapsed_time(b) for a, b in evs)[len(evs) // 2]
+    nbytes, flops = warmnet_bytes_flops(W, H, L)
+    xb = torch.rand((16, 192, 256, L), device="cuda", generator=gen) * 4
+    tb = xb + 0.1 * torch.rand(xb.shape, device="cuda", generator=gen)
+    for _ in range(args.warmup):
+        net.train_step(xb, tb, lr=1e-4, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        net.train_step(xb, tb, lr=1e-4, stream=stream.cuda_stream)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    ms_train = t0.elapsed_time(t1) / args.steps
+    hbm, hbm_src = load_peaks()
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            tfl = float(json.load(f)["bf16_tflops"])
+    except Exception:
+        tfl = 1900.0
+    achieved = nbytes / (ms / 1e3) / 1e9
+    line = {"metric": "warm-start network forward, 960x540x64 (ms per call)", "value": round(ms, 4), "unit": "ms",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)",
+            "data": "synthetic (uniform inputs, seeded random weights)",
+            "config": {"workload": cfg["name"], "width": W, "height": H, "labels": L, "hidden": 32,
+                       "layers": "conv3x3 L->32->32->32->L, ReLU, residual", "gflop": round(flops / 1e9, 2),
+                       "algorithmic_mb": round(nbytes / 1e6, 1)},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                         "frac": round(achieved / hbm, 4), "traffic": None, "peak_source": hbm_src,
+                         "note": "whole forward call (5 kernels, host return included) over its algorithmic bytes"},
+            "tensor_tflops": round(flops / (ms / 1e3) / 1e12, 1), "tensor_peak_tflops": tfl,
+            "train_step_ms": round(ms_train, 3),
+            "train_step_batch": "16 x 192x256x64 (level 1 of 512x384 grids)",
+            "gpu_launches": 5}
+    print(json.dumps(line), flush=True)
+    net.close()
+
+
 # ---------------------------------------------------------------- reference arm
 
 def run_reference(args, cfg):
@@ -902,6 +987,10 @@ def main():
         import gridinfcuda_gb300
         gridinfcuda_gb300.build()
         run_alphabeta(args, cfg)
+    elif args.workload == "warmnet":
+        import gridinfcuda_gb300
+        gridinfcuda_gb300.build()
+        run_warmnet(args, cfg)
     elif args.workload == "quad":
         import gridinfcuda_gb300
         gridinfcuda_gb300.build()

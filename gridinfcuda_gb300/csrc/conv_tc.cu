@@ -9,16 +9,18 @@
 // FP32 accumulation.  Activations are NHWC BF16.  A CTA owns a strip of
 // tiles going down one 128-pixel column band of an image, so each input row
 // is loaded once (plus one halo row above and below the strip): a row
-// arrives as CIN/8 TMA copies of 130 pixels x 8 channels (the band plus one
-// pixel either side; pixels and rows outside the image read as zero, which
-// is the convolution's zero padding), landing in the canonical K-major
-// layout without swizzle: per 8-channel chunk a slab of 130 pixel rows of
-// 16 bytes (slabs 2176 bytes apart, so that each copy starts 128-byte
-// aligned).  Eight consecutive pixels of a slab are one 8x16-byte core
-// matrix, so the A operand of tap (dy, dx) is the slab of row y + dy read
-// from pixel dx + 1 on -- the nine taps are nine descriptors over three row
-// buffers, nothing is copied per tap.  The weights, [tap][chunk][co][8] in
-// the same layout, stay in shared memory for the CTA's life.
+// arrives as one TMA tensor copy of 130 pixels x CIN channels (the band plus
+// one pixel either side; pixels and rows outside the image read as zero,
+// which is the convolution's zero padding) into a 1024-byte aligned buffer,
+// swizzled by the copy (128-, 64- or 32-byte swizzle for CIN = 64, 32, 16:
+// one pixel's channels per swizzle row), which is the canonical K-major
+// layout the tensor cores read: 8-pixel groups SBO = 8 rows apart.  The
+// swizzle is a function of the absolute shared-memory address, so the A
+// operand of tap (dy, dx) is the buffer of row y + dy read from pixel dx + 1
+// on, a descriptor whose start is one swizzle row further per pixel -- the
+// nine taps are nine descriptors over three row buffers, nothing is copied
+// per tap.  The weights, [tap][8-channel chunk][co][8] in the canonical
+// layout without swizzle, stay in shared memory for the CTA's life.
 //
 // Roles (192 threads): warp 4 lane 0 issues the row copies into a ring of
 // RING buffers; warp 5 lane 0 issues the 9 * CIN / 16 MMAs of a tile into one
@@ -54,7 +56,6 @@ namespace {
 
 constexpr int kTileM = 128;            // pixels per tile (MMA M)
 constexpr int kSlab = kTileM + 2;      // pixels per row copy: the band and one either side
-constexpr int kPitch = 136 * 16;       // bytes between chunk slabs (a copy's destination is 128-byte aligned)
 constexpr int kThreadsTc = 192;        // warps 0-3 epilogue, 4 copies, 5 MMA
 constexpr int kCopyWarp = 4, kMmaWarp = 5;
 
@@ -62,22 +63,23 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
-// One box of the 5-D row map (8 channels, chunk, x, row, image).
-__device__ __forceinline__ void tma_load_row(uint32_t dst, const CUtensorMap *map, int chunk, int x, int row, int img,
+// One box of the 4-D row map (channels, x, row, image): a row of the band.
+__device__ __forceinline__ void tma_load_row(uint32_t dst, const CUtensorMap *map, int x, int row, int img,
                                              uint64_t *bar) {
     asm volatile(
-        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
-        "%6}], [%7];" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(chunk), "r"(x), "r"(row), "r"(img), "r"(smem_addr(bar))
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(x), "r"(row), "r"(img), "r"(smem_addr(bar))
         : "memory");
 }
 
-// Shared-memory matrix descriptor, canonical layout without swizzle: start
-// address, leading byte offset (between core matrices adjacent in K), stride
-// byte offset (between core matrices adjacent in M or N), version 1.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+// Shared-memory matrix descriptor: start address, leading byte offset
+// (between core matrices adjacent in K; unused when a swizzle row holds the
+// instruction's K), stride byte offset (between 8-row groups in M or N),
+// version 1, swizzle mode (0 none, 2 128-byte, 4 64-byte, 6 32-byte).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo, uint32_t swizzle = 0) {
     return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
-           (1ull << 46);
+           (1ull << 46) | ((uint64_t)swizzle << 61);
 }
 
 // Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
@@ -138,8 +140,10 @@ __device__ __forceinline__ Item item_of(const ConvTcParams &p, int it) {
 template <int CIN, int COUT, bool OUT_F32, int RING>
 struct TcLayout {
     static constexpr int kChunks = CIN / 8;
-    static constexpr int kRowBytes = kChunks * kPitch;      // one row buffer: [chunk][130 pixels + pad][16 B]
-    static constexpr int kCopyBytes = kChunks * kSlab * 16;  // what one row's copies write
+    static constexpr int kPixBytes = CIN * 2;                          // one pixel: one swizzle row
+    static constexpr uint32_t kSwizzle = CIN == 64 ? 2 : (CIN == 32 ? 4 : 6);
+    static constexpr int kCopyBytes = kSlab * kPixBytes;               // what one row's copy writes
+    static constexpr int kRowBytes = (kCopyBytes + 1023) / 1024 * 1024;  // one row buffer, 1024-byte aligned
     static constexpr int kWBytes = 9 * CIN * COUT * 2;      // [tap][chunk][co][16 B]
     static constexpr int kRows = 0;
     static constexpr int kW = kRows + RING * kRowBytes;
@@ -149,33 +153,46 @@ struct TcLayout {
     static constexpr int kStagePitch = kOutBytes + 16;
     static constexpr int kStage = (kBias + COUT * 4 + 15) / 16 * 16;  // 4 warps x 32 pixel rows
     static constexpr int kBars = kStage + 4 * 32 * kStagePitch;
-    static constexpr int kNumBars = 2 * RING + 5;  // full[RING], empty[RING], acc_full[2], acc_empty[2], done
+    static constexpr int kAcc = COUT == 64 ? 4 : 8;  // accumulator slots in tensor memory
+    static constexpr int kNumBars = 2 * RING + 2 * kAcc + 1;  // full, empty, acc_full, acc_empty, done
     static constexpr int kTmemSlot = kBars + kNumBars * 8;
     static constexpr int kAbort = kTmemSlot + 4;
     static constexpr int kBytes = kAbort + 4;
-    static constexpr uint32_t kCols = 2 * COUT < 32 ? 32 : 2 * COUT;  // two accumulators, a power of two >= 32
+    static constexpr uint32_t kCols = kAcc * COUT;  // 128 or 256 columns: two CTAs fit an SM's 512
+    static_assert((kCols & (kCols - 1)) == 0 && kCols >= 32, "tensor-memory allocation is a power of two");
 };
 
+// Tensor-memory column of output row (tile) t's accumulator: slots run
+// downwards, so the accumulators of rows r + 1, r, r - 1 -- the three an
+// input row r feeds -- are adjacent and ascending unless the ring wraps.
+template <int COUT, int ACC>
+__device__ __forceinline__ uint32_t acc_col(uint32_t t) {
+    return (uint32_t)(ACC - 1 - (int)(t % ACC)) * COUT;
+}
+
 template <int CIN, int COUT, bool RELU, bool OUT_F32, int RING>
-__global__ void __launch_bounds__(kThreadsTc, 1)
+__global__ void __launch_bounds__(kThreadsTc, 2)
     k_conv_tc(const __grid_constant__ CUtensorMap rows_map, const ConvTcParams p) {
     using Lay = TcLayout<CIN, COUT, OUT_F32, RING>;
-    static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 256, "tile shape");
+    static_assert((CIN == 16 || CIN == 32 || CIN == 64) && COUT % 16 == 0 && COUT <= 256, "tile shape");
     extern __shared__ __align__(1024) unsigned char sm[];
     uint64_t *bars = reinterpret_cast<uint64_t *>(sm + Lay::kBars);
-    uint64_t *full = bars, *empty = bars + RING, *acc_full = bars + 2 * RING, *acc_empty = acc_full + 2,
-             *done = acc_empty + 2;
+    uint64_t *full = bars, *empty = bars + RING, *acc_full = bars + 2 * RING, *acc_empty = acc_full + Lay::kAcc,
+             *done = acc_empty + Lay::kAcc;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + Lay::kTmemSlot);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(sm + Lay::kAbort);
     float *bias = reinterpret_cast<float *>(sm + Lay::kBias);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned char *stage = sm + Lay::kStage + (warp & 3) * 32 * Lay::kStagePitch;
 
-    // Weights into [tap][chunk][co][8 channels], the bias (zero without one).
+    // Weights into [dx][chunk][j * COUT + co][8 channels]: for one column
+    // offset dx the three row offsets dy = j - 1 stacked along N, so one MMA
+    // applies all three to an input row.  The bias (zero without one).
     for (int e = threadIdx.x; e < 9 * Lay::kChunks * COUT; e += blockDim.x) {
-        const int co = e % COUT, t = e / COUT, c8 = t % Lay::kChunks, tap = t / Lay::kChunks;
+        const int n = e % (3 * COUT), t = e / (3 * COUT), c8 = t % Lay::kChunks, dx = t / Lay::kChunks;
+        const int j = n / COUT, co = n % COUT;
         *reinterpret_cast<uint4 *>(sm + Lay::kW + (size_t)e * 16) =
-            *reinterpret_cast<const uint4 *>(p.wt + ((size_t)co * 9 + tap) * CIN + c8 * 8);
+            *reinterpret_cast<const uint4 *>(p.wt + ((size_t)co * 9 + j * 3 + dx) * CIN + c8 * 8);
     }
     for (int c = threadIdx.x; c < COUT; c += blockDim.x) bias[c] = p.bias ? p.bias[c] : 0.f;
     if (threadIdx.x == 0) {
@@ -183,7 +200,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], 1);
         }
-        for (int i = 0; i < 2; ++i) {
+        for (int i = 0; i < Lay::kAcc; ++i) {
             mbar_init(&acc_full[i], 1);
             mbar_init(&acc_empty[i], 4 * 32);
         }
@@ -202,7 +219,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    if (smem_addr(sm) & 127u) {  // row copies need 128-byte aligned destinations
+    if (smem_addr(sm) & 1023u) {  // swizzled row buffers start on 1024-byte boundaries
         if (threadIdx.x == 0 && p.status) atomicOr(p.status, DEV_ERR_BOUNDS);
         *abort_flag = 1;
     }
@@ -220,10 +237,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
                         break;
                     }
                     mbar_arrive_expect_tx(&full[slot], Lay::kCopyBytes);
-                    const uint32_t dst = smem_addr(sm + Lay::kRows + slot * Lay::kRowBytes);
-#pragma unroll
-                    for (int c = 0; c < Lay::kChunks; ++c)
-                        tma_load_row(dst + c * kPitch, &rows_map, c, t.x0 - 1, r, t.img, &full[slot]);
+                    tma_load_row(smem_addr(sm + Lay::kRows + slot * Lay::kRowBytes), &rows_map, t.x0 - 1, r, t.img,
+                                 &full[slot]);
                 }
             }
             // Copies still in flight land before the CTA's shared memory goes.
@@ -233,47 +248,61 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
         __syncwarp();
     } else if (warp == kMmaWarp) {
         if (lane == 0) {
-            constexpr uint32_t idesc = instr_desc_bf16(COUT);
-            const uint32_t wbase = smem_addr(sm + Lay::kW), rbase = smem_addr(sm + Lay::kRows);
+            constexpr int ACC = Lay::kAcc;
+            const uint32_t rbase = smem_addr(sm + Lay::kRows);
+            // Weights: [dx][chunk][3 * COUT rows][16 B], K-adjacent chunks 3 * COUT * 16 bytes apart.
+            const uint64_t bdesc = smem_desc(smem_addr(sm + Lay::kW), 3 * COUT * 16, 128);
             uint32_t ld = 0, tile = 0;
             bool ok = true;
             for (int it = blockIdx.x; it < p.items && ok && !*abort_flag; it += gridDim.x) {
                 const Item t = item_of(p, it);
-                const uint32_t base = ld;
-                for (int j = 0; j < t.rows && ok; ++j, ++tile) {
-                    // Rows y - 1, y, y + 1 of output row y = y0 + j are copies base + j .. base + j + 2.
-                    for (uint32_t q = j == 0 ? base : base + j + 2; q <= base + j + 2 && ok; ++q)
-                        ok = mbar_wait_bounded(&full[q % RING], (q / RING) & 1u, p.status);
-                    const uint32_t acc = tile & 1u;
-                    if (ok) ok = mbar_wait_bounded(&acc_empty[acc], ((tile >> 1) & 1u) ^ 1u, p.status);
+                // Input row r = y0 - 1 + i feeds output rows y = r + 1 - j
+                // (dy = j - 1), j in [jlo, jhi] within the strip; output row
+                // y0 + m is tile `tile + m`.
+                for (int i = 0; i < t.rows + 2 && ok; ++i, ++ld) {
+                    const int jlo = i - (t.rows - 1) > 0 ? i - (t.rows - 1) : 0, jhi = i < 2 ? i : 2;
+                    ok = mbar_wait_bounded(&full[ld % RING], (ld / RING) & 1u, p.status);
+                    // Block j = 0 starts row y0 + i's accumulator: its slot must be read out.
+                    if (ok && jlo == 0) {
+                        const uint32_t tn = tile + i;
+                        ok = mbar_wait_bounded(&acc_empty[tn % ACC], ((tn / ACC) & 1u) ^ 1u, p.status);
+                    }
                     if (!ok) break;
                     tc_fence_after();
-                    const uint32_t d = tmem + acc * COUT;
-                    uint32_t accumulate = 0;
+                    // The blocks j in [jlo, jhi] as at most two runs with
+                    // adjacent accumulators (the ring wraps at most once),
+                    // fixed for the row; every step then issues one MMA per
+                    // run, its descriptors the row's plus constant offsets.
+                    int k0 = jlo;
+                    while (k0 < jhi && (tile + i - k0) % ACC != 0) ++k0;
+                    const int n0 = k0 - jlo + 1, n1 = jhi - k0;  // blocks in run 0, run 1
+                    const uint32_t d0 = tmem + acc_col<COUT, ACC>(tile + i - jlo);
+                    const uint32_t d1 = tmem + acc_col<COUT, ACC>(tile + i - k0 - 1);
+                    const uint32_t i0 = instr_desc_bf16(n0 * COUT), i1 = instr_desc_bf16(n1 > 0 ? n1 * COUT : 16);
+                    const uint64_t a0 = smem_desc(rbase + (ld % RING) * Lay::kRowBytes, 16, 8 * Lay::kPixBytes,
+                                                  Lay::kSwizzle);
+                    const uint64_t b0 = bdesc + (uint64_t)(jlo * COUT), b1 = bdesc + (uint64_t)((k0 + 1) * COUT);
 #pragma unroll
-                    for (int dy = 0; dy < 3; ++dy) {
-                        const uint32_t row = rbase + ((base + j + dy) % RING) * Lay::kRowBytes;
+                    for (int dx = 0; dx < 3; ++dx)
 #pragma unroll
-                        for (int dx = 0; dx < 3; ++dx)
-#pragma unroll
-                            for (int ks = 0; ks < CIN / 16; ++ks) {
-                                const uint64_t a = smem_desc(row + 2 * ks * kPitch + dx * 16, kPitch, 128);
-                                const uint64_t b =
-                                    smem_desc(wbase + (((dy * 3 + dx) * Lay::kChunks + 2 * ks) * COUT) * 16, COUT * 16, 128);
-                                umma_bf16(d, a, b, idesc, accumulate);
-                                accumulate = 1;
+                        for (int ks = 0; ks < CIN / 16; ++ks) {
+                            // Offsets in 16-byte units of the descriptors' address fields.
+                            const uint64_t ao = (uint64_t)((dx * Lay::kPixBytes + ks * 32) >> 4);
+                            const uint64_t bo = (uint64_t)((dx * Lay::kChunks + 2 * ks) * 3 * COUT);
+                            if (dx == 0 && ks == 0 && jlo == 0) {
+                                // Block 0 starts output row y0 + i: overwrite.
+                                umma_bf16(d0, a0, b0, instr_desc_bf16(COUT), 0u);
+                                if (n0 > 1)
+                                    umma_bf16(d0 + COUT, a0, b0 + (uint64_t)COUT, instr_desc_bf16((n0 - 1) * COUT), 1u);
+                            } else {
+                                umma_bf16(d0, a0 + ao, b0 + bo, i0, 1u);
                             }
-                    }
-                    umma_commit(&acc_full[acc]);
-                    // Copy base + j (row y - 1) has had its last tile; after the
-                    // strip's last tile so have the two below it.
-                    umma_commit(&empty[(base + j) % RING]);
-                    if (j == t.rows - 1) {
-                        umma_commit(&empty[(base + j + 1) % RING]);
-                        umma_commit(&empty[(base + j + 2) % RING]);
-                    }
+                            if (n1 > 0) umma_bf16(d1, a0 + ao, b1 + bo, i1, 1u);
+                        }
+                    umma_commit(&empty[ld % RING]);  // the row's only MMAs are these
+                    if (jhi == 2) umma_commit(&acc_full[(tile + i - 2) % ACC]);  // row y0 + i - 2 is done
                 }
-                ld = base + t.rows + 2;
+                tile += t.rows;
             }
             if (!ok) *abort_flag = 1;
             umma_commit(done);
@@ -289,15 +318,16 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
         for (int it = blockIdx.x; it < p.items && !__any_sync(~0u, *abort_flag); it += gridDim.x) {
             const Item t = item_of(p, it);
             for (int j = 0; j < t.rows; ++j, ++tile) {
-                const uint32_t acc = tile & 1u;
-                if (!__all_sync(~0u, mbar_wait_bounded(&acc_full[acc], (tile >> 1) & 1u, p.status))) {
+                const uint32_t acc = tile % Lay::kAcc;
+                if (!__all_sync(~0u, mbar_wait_bounded(&acc_full[acc], (tile / Lay::kAcc) & 1u, p.status))) {
                     *abort_flag = 1;
                     break;
                 }
                 tc_fence_after();
                 float v[COUT];
 #pragma unroll
-                for (int c = 0; c < COUT; c += 16) tmem_load16(tmem + lane_base + acc * COUT + c, v + c);
+                for (int c = 0; c < COUT; c += 16)
+                    tmem_load16(tmem + lane_base + acc_col<COUT, Lay::kAcc>(tile) + c, v + c);
                 tc_fence_before();
                 mbar_arrive(&acc_empty[acc]);
 #pragma unroll
@@ -390,32 +420,48 @@ cudaError_t launch_conv_tc(const __nv_bfloat16 *in, ConvTcParams p, cudaStream_t
     constexpr int kFit = (kBudget - kFixed) / TcLayout<CIN, COUT, OUT_F32, 8>::kRowBytes;
     constexpr int RING = kFit < 3 ? 3 : (kFit > 8 ? 8 : kFit);
     using Lay = TcLayout<CIN, COUT, OUT_F32, RING>;
+    // At least 80 KB, so that no more than two CTAs share an SM's 512
+    // tensor-memory columns (a third would wait in its allocation).
+    constexpr int kSmem = Lay::kBytes < 80 * 1024 ? 80 * 1024 : Lay::kBytes;
     auto kern = k_conv_tc<CIN, COUT, RELU, OUT_F32, RING>;
     static std::once_flag once;
     static cudaError_t attr_err = cudaSuccess;
     std::call_once(once, [&] {
-        attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::kBytes);
+        attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
+        // Without a carveout preference the occupancy query assumes a smaller
+        // shared-memory split and sizes the grid for one CTA per SM.
+        if (attr_err == cudaSuccess)
+            attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                            (int)cudaSharedmemCarveoutMaxShared);
     });
     if (attr_err != cudaSuccess) return attr_err;
     PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
     if (!encode) return cudaErrorNotSupported;
-    // Rows map over the NHWC input: (8 channels, chunk, x, row, image), packed strides.
+    // Rows map over the NHWC input (channels, x, row, image), swizzled by a pixel's bytes.
     alignas(64) CUtensorMap map;
-    const cuuint64_t dims[5] = {8, (cuuint64_t)(CIN / 8), (cuuint64_t)p.w, (cuuint64_t)p.h, (cuuint64_t)p.n};
-    const cuuint64_t strides[4] = {16, (cuuint64_t)CIN * 2, (cuuint64_t)p.w * CIN * 2, (cuuint64_t)p.h * p.w * CIN * 2};
-    const cuuint32_t box[5] = {8, 1, kSlab, 1, 1};
-    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
-    if (encode(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<__nv_bfloat16 *>(in), dims, strides, box, estr,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+    const cuuint64_t dims[4] = {(cuuint64_t)CIN, (cuuint64_t)p.w, (cuuint64_t)p.h, (cuuint64_t)p.n};
+    const cuuint64_t strides[3] = {(cuuint64_t)CIN * 2, (cuuint64_t)p.w * CIN * 2, (cuuint64_t)p.h * p.w * CIN * 2};
+    const cuuint32_t box[4] = {(cuuint32_t)CIN, kSlab, 1, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUtensorMapSwizzle swz =
+        CIN == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : (CIN == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B);
+    if (encode(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16 *>(in), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
-    int dev = 0, sms = 0, per_sm = 0;
+    int dev = 0, sms = 0, smem_sm = 0, reserved = 0;
     cudaError_t e;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreadsTc, Lay::kBytes)) != cudaSuccess)
+    if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess)
         return e;
-    const int slots = sms * (per_sm > 0 ? per_sm : 1);
+    if ((e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess)
+        return e;
+    // CTAs per SM from shared memory (registers allow two by the launch
+    // bounds); the occupancy query under-reports this kernel's.
+    int per_sm = smem_sm / (kSmem + reserved);
+    per_sm = per_sm < 1 ? 1 : (per_sm > 2 ? 2 : per_sm);
+    const int slots = sms * per_sm;
     // Split each band's rows into chunks so that the items about fill the GPU
     // once, keeping at least four rows per chunk (two halo rows per chunk).
     p.bands = (p.w + kTileM - 1) / kTileM;
@@ -429,7 +475,7 @@ cudaError_t launch_conv_tc(const __nv_bfloat16 *in, ConvTcParams p, cudaStream_t
     if (items > 0x7fffffffLL) return cudaErrorInvalidValue;
     p.items = (int)items;
     const int grid = p.items < slots ? p.items : slots;
-    kern<<<grid, kThreadsTc, Lay::kBytes, s>>>(map, p);
+    kern<<<grid, kThreadsTc, kSmem, s>>>(map, p);
     return cudaGetLastError();
 }
 

@@ -249,7 +249,6 @@ struct ginf_warmnet {
     // activations / gradients, grown to the largest batch seen
     size_t cap_pix = 0;
     __nv_bfloat16 *a[4] = {};  // a[0] = x (L ch), a[1..3] hidden
-    float *x32 = nullptr;      // residual input (FP32 copy of x)
     float *y = nullptr;        // output (L ch)
     float *gy = nullptr;       // dLoss/dy
     float *g32 = nullptr;      // FP32 gradient scratch (max channels)
@@ -330,7 +329,6 @@ ginf_status refresh_bf16(ginf_warmnet *n, cudaStream_t s) {
 ginf_status ensure_batch(ginf_warmnet *n, size_t pix) {
     if (pix <= n->cap_pix) return GINF_OK;
     for (int l = 0; l < 4; ++l) cudaFree(n->a[l]);
-    cudaFree(n->x32);
     cudaFree(n->y);
     cudaFree(n->gy);
     cudaFree(n->g32);
@@ -339,7 +337,6 @@ ginf_status ensure_batch(ginf_warmnet *n, size_t pix) {
     const size_t cmax = (size_t)std::max(n->L, n->hidden);
     GINF_WCK(cudaMalloc(&n->a[0], pix * n->L * sizeof(__nv_bfloat16)));
     for (int l = 1; l < 4; ++l) GINF_WCK(cudaMalloc(&n->a[l], pix * n->hidden * sizeof(__nv_bfloat16)));
-    GINF_WCK(cudaMalloc(&n->x32, pix * n->L * sizeof(float)));
     GINF_WCK(cudaMalloc(&n->y, pix * n->L * sizeof(float)));
     GINF_WCK(cudaMalloc(&n->gy, pix * n->L * sizeof(float)));
     GINF_WCK(cudaMalloc(&n->g32, pix * cmax * sizeof(float)));
@@ -377,18 +374,19 @@ cudaError_t conv_wgrad(int cin, int cout, const __nv_bfloat16 *dout, const __nv_
     return cudaErrorInvalidValue;
 }
 
-ginf_status forward(ginf_warmnet *n, const float *x, Geo g, int *status, cudaStream_t s) {
+// y = x + net(x) into y_out (the network's own buffer when null); the last
+// layer reads x itself as its residual.
+ginf_status forward(ginf_warmnet *n, const float *x, Geo g, int *status, cudaStream_t s, float *y_out = nullptr) {
     const size_t pix = (size_t)g.n * g.h * g.w;
     ginf_status st = ensure_batch(n, pix);
     if (st != GINF_OK) return st;
-    GINF_WCK(cudaMemcpyAsync(n->x32, x, pix * n->L * sizeof(float), cudaMemcpyDeviceToDevice, s));
     k_f32_to_bf16<<<nblocks(pix * n->L), kThreads, 0, s>>>(x, n->a[0], pix * n->L);
     GINF_WCK(cudaGetLastError());
     for (int l = 0; l < 3; ++l)
         GINF_WCK(conv_fwd(n->cin[l], n->cout[l], true, false, n->a[l], n->wbf + n->woff[l], n->params + n->boff[l], g,
                           n->a[l + 1], nullptr, status, s));
     GINF_WCK(conv_fwd(n->cin[3], n->cout[3], false, true, n->a[3], n->wbf + n->woff[3], n->params + n->boff[3], g,
-                      n->y, n->x32, status, s));
+                      y_out ? y_out : n->y, x, status, s));
     return GINF_OK;
 }
 
@@ -456,6 +454,14 @@ ginf_status warmnet_forward(ginf_warmnet *n, const float *x, int nimg, int h, in
     *y_out = n->y;
     return GINF_OK;
 }
+
+// The C-ABI forward: the last layer writes the caller's buffer.
+ginf_status warmnet_forward_into(ginf_warmnet *n, const float *x, int nimg, int h, int w, float *out, cudaStream_t s) {
+    ginf_status st = check_geo(n, nimg, h, w);
+    if (st != GINF_OK) return st;
+    Geo g{nimg, h, w};
+    return forward(n, x, g, n->status, s, out);
+}
 int warmnet_labels(const ginf_warmnet *n) { return n ? n->L : 0; }
 }  // namespace ginf_gpu
 
@@ -505,7 +511,6 @@ ginf_status ginf_warmnet_destroy(ginf_warmnet *n) {
     cudaFree(n->wbf);
     cudaFree(n->wflip);
     for (int l = 0; l < 4; ++l) cudaFree(n->a[l]);
-    cudaFree(n->x32);
     cudaFree(n->y);
     cudaFree(n->gy);
     cudaFree(n->g32);
@@ -543,11 +548,9 @@ ginf_status ginf_warmnet_set_params(ginf_warmnet *n, const float *host) {
 ginf_status ginf_warmnet_forward(ginf_warmnet *n, const float *x, int32_t nimg, int32_t h, int32_t w, float *out,
                                  void *stream) {
     ginf_gpu::set_last_error("");
-    float *y = nullptr;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    ginf_status st = warmnet_forward(n, x, nimg, h, w, &y, nullptr, s);
+    ginf_status st = warmnet_forward_into(n, x, nimg, h, w, out, s);
     if (st != GINF_OK) return st;
-    GINF_WCK(cudaMemcpyAsync(out, y, (size_t)nimg * h * w * n->L * sizeof(float), cudaMemcpyDeviceToDevice, s));
     GINF_WCK(cudaStreamSynchronize(s));
     return check_status(n);
 }

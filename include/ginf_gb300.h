@@ -282,6 +282,8 @@ ginf_status ginf_warmnet_num_params(const ginf_warmnet *net, int64_t *count);
 /* FP32 parameters, per layer the weights [cout][3][3][cin] then the biases. */
 ginf_status ginf_warmnet_get_params(const ginf_warmnet *net, float *host);
 ginf_status ginf_warmnet_set_params(ginf_warmnet *net, const float *host);
+/* y = x + net(x).  x, y 16-byte aligned (GINF_ERR_CUDA otherwise); y may be x.
+ * The convolutions run on tcgen05 with tensor-memory accumulators. */
 ginf_status ginf_warmnet_forward(ginf_warmnet *net, const float *x, int32_t n, int32_t h, int32_t w, float *y,
                                  void *stream);
 /* Mean-squared-error loss against target and the gradient of every
