@@ -137,9 +137,26 @@ __global__ void k_flip_weights(const __nv_bfloat16 *__restrict__ w, int cin, int
     wf[i] = w[((size_t)co * 9 + (8 - tap)) * cin + ci];
 }
 
+// Round to BF16, eight values per thread (two 16-byte loads, one 16-byte
+// store) when both buffers are 16-byte aligned, grid-stride, scalar tail.
 __global__ void k_f32_to_bf16(const float *__restrict__ a, __nv_bfloat16 *__restrict__ b, size_t n) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) b[i] = __float2bfloat16_rn(a[i]);
+    const size_t n8 = (((uintptr_t)a | (uintptr_t)b) & 15) == 0 ? n / 8 : 0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (size_t i = t; i < n8; i += stride) {
+        const float4 lo = reinterpret_cast<const float4 *>(a)[2 * i], hi = reinterpret_cast<const float4 *>(a)[2 * i + 1];
+        reinterpret_cast<uint4 *>(b)[i] =
+            make_uint4(pack_bf16(__float2bfloat16_rn(lo.x), __float2bfloat16_rn(lo.y)),
+                       pack_bf16(__float2bfloat16_rn(lo.z), __float2bfloat16_rn(lo.w)),
+                       pack_bf16(__float2bfloat16_rn(hi.x), __float2bfloat16_rn(hi.y)),
+                       pack_bf16(__float2bfloat16_rn(hi.z), __float2bfloat16_rn(hi.w)));
+    }
+    for (size_t i = n8 * 8 + t; i < n; i += stride) b[i] = __float2bfloat16_rn(a[i]);
+}
+
+void f32_to_bf16(const float *a, __nv_bfloat16 *b, size_t n, cudaStream_t s) {
+    const size_t blocks = (n / 8 + kThreads - 1) / kThreads;
+    k_f32_to_bf16<<<(unsigned)(blocks < 1 ? 1 : (blocks > 4096 ? 4096 : blocks)), kThreads, 0, s>>>(a, b, n);
 }
 
 // Loss = mean((y - t)^2) (per-block double partials), dy = 2 (y - t) / n.
@@ -321,7 +338,7 @@ ginf_status check_status(ginf_warmnet *n) {
 }
 
 ginf_status refresh_bf16(ginf_warmnet *n, cudaStream_t s) {
-    k_f32_to_bf16<<<nblocks(n->nparams), kThreads, 0, s>>>(n->params, n->wbf, n->nparams);
+    f32_to_bf16(n->params, n->wbf, n->nparams, s);
     GINF_WCK(cudaGetLastError());
     return GINF_OK;
 }
@@ -380,7 +397,7 @@ ginf_status forward(ginf_warmnet *n, const float *x, Geo g, int *status, cudaStr
     const size_t pix = (size_t)g.n * g.h * g.w;
     ginf_status st = ensure_batch(n, pix);
     if (st != GINF_OK) return st;
-    k_f32_to_bf16<<<nblocks(pix * n->L), kThreads, 0, s>>>(x, n->a[0], pix * n->L);
+    f32_to_bf16(x, n->a[0], pix * n->L, s);
     GINF_WCK(cudaGetLastError());
     for (int l = 0; l < 3; ++l)
         GINF_WCK(conv_fwd(n->cin[l], n->cout[l], true, false, n->a[l], n->wbf + n->woff[l], n->params + n->boff[l], g,
@@ -401,7 +418,7 @@ ginf_status backward(ginf_warmnet *n, const float *target, Geo g, cudaStream_t s
     const int chunks = (int)((pix + kChunk - 1) / kChunk);
     // Layer 4 (linear output): g = dy.
     const float *gl = n->gy;
-    k_f32_to_bf16<<<nblocks(ny), kThreads, 0, s>>>(n->gy, n->gb, ny);
+    f32_to_bf16(n->gy, n->gb, ny, s);
     GINF_WCK(cudaGetLastError());
     for (int l = 3; l >= 0; --l) {
         const int ci = n->cin[l], co = n->cout[l];
