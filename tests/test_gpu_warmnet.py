@@ -237,3 +237,52 @@ def test_trained_network_beats_the_network_free_guess(ginf):
     got = float(((pred - Yh) ** 2).mean())
     assert hist[-1] < hist[0]
     assert got < 0.93 * base, (got, base)
+
+
+def _torch_forward(params, x, L):
+    """Plain PyTorch float64 forward of the network, rounding to BF16 where
+    the library does: x, the weights and the three hidden activations.  x is
+    (n, h, w, L) on the GPU; returns y = x + net(x), (n, h, w, L)."""
+    import torch
+    bf = lambda t: t.to(torch.bfloat16).to(torch.float64)
+    p = torch.from_numpy(np.asarray(params, np.float64)).cuda()
+    a = bf(x.double()).permute(0, 3, 1, 2)
+    off = 0
+    for layer, (cin, cout) in enumerate(REF.shapes(L)):
+        nw = cout * 9 * cin
+        w = bf(p[off:off + nw].reshape(cout, 3, 3, cin).permute(0, 3, 1, 2).contiguous())
+        b = p[off + nw:off + nw + cout]
+        off += nw + cout
+        a = torch.nn.functional.conv2d(a, w, b, padding=1)
+        if layer < 3:
+            a = bf(torch.relu(a))
+    return x.double() + a.permute(0, 2, 3, 1)
+
+
+@pytest.mark.parametrize("L", [16, 32, 64])
+@pytest.mark.parametrize("shape", [(2, 720, 256), (1, 37, 300), (200, 5, 20)])
+def test_tcgen05_convolutions_at_scale(ginf, L, shape):
+    """The tcgen05 convolutions against a plain PyTorch float64 reference at
+    sizes the small oracle tests do not reach: 2 x 720 x 256 gives each CTA
+    more rows than either accumulator ring holds (8 slots at COUT 16 / 32, 4
+    at 64), so the ring wraps; 1 x 37 x 300 ends in a 44-pixel band; 200
+    images of 5 x 20 give more work items than CTA slots, so CTAs carry their
+    tile and row-copy counters across items.  Forward within 1e-4
+    (norm-relative), as the oracle test; the data-gradient path (the same
+    kernel with flipped weights and FP32 output) is exercised through
+    `gradients` and checked for finiteness and agreement between two runs."""
+    import torch
+    n, h, w = shape
+    params = REF.init_params(L, seed=3 + L)
+    gen = torch.Generator(device="cuda").manual_seed(n * h + w + L)
+    x = torch.rand((n, h, w, L), device="cuda", generator=gen)
+    with ginf.WarmNet(L, 32) as net:
+        net.set_params(params)
+        y = net.forward(x)
+        t = x + 0.05 * torch.rand(x.shape, device="cuda", generator=gen)
+        loss1, g1 = net.gradients(x, t)
+        loss2, g2 = net.gradients(x, t)
+    want = _torch_forward(params, x, L)
+    assert _rel(y.cpu().numpy(), want.cpu().numpy()) < 1e-4
+    assert np.isfinite(loss1) and np.all(np.isfinite(g1))
+    assert loss1 == loss2 and np.array_equal(g1, g2)
