@@ -1,8 +1,8 @@
-// conv_tc.cu -- the warm-start network's 3x3 convolution (the forward pass,
-// and the data gradient as a forward convolution with flipped weights) on the
-// fifth-generation tensor cores: tcgen05.mma with the accumulator in tensor
-// memory, both operands read from shared memory by matrix descriptors, the
-// input rows brought in by TMA tensor copies.
+// conv_tc.cu -- the warm-start network's 3x3 convolutions (the forward pass,
+// the data gradient as a forward convolution with flipped weights, and the
+// weight gradient) on the fifth-generation tensor cores: tcgen05.mma with the
+// accumulator in tensor memory, both operands read from shared memory by
+// matrix descriptors, the input rows brought in by TMA tensor copies.
 //
 // Implicit GEMM.  A tile is M = 128 consecutive pixels of one image row,
 // N = COUT output channels, K = 9 taps x CIN input channels, BF16 operands,
@@ -479,6 +479,287 @@ cudaError_t launch_conv_tc(const __nv_bfloat16 *in, ConvTcParams p, cudaStream_t
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Weight gradient: dW[co][tap][ci] = sum over pixels p of dout[p][co] *
+// in[p shifted by tap][ci], a GEMM with the pixels as K.  Both operands are
+// read MN-major (channels contiguous per pixel) from the same swizzled row
+// buffers the forward pass uses: A = input rows, M = taps x CIN, where one
+// M = 128 tile holds 128 / CIN taps of one row offset dy as MN atoms one
+// pixel apart (LBO = a pixel's bytes; the taps past dx = +1 are computed and
+// dropped); B = the output-gradient row [128 pixels][COUT], N = COUT.  Each
+// CTA accumulates in tensor memory over all of its rows (K steps of 16
+// pixels) and writes one partial sum; the caller adds the partials in a
+// fixed order, so the result is deterministic.
+
+struct WgradParams {
+    float *partials;  // [CTA][COUT][9][CIN]
+    int n, h, w;
+    int bands, chunks, rows_per_chunk, items;
+    int *status;
+};
+
+template <int CIN, int COUT, int RING>
+struct WgLayout {
+    static constexpr int kInPix = CIN * 2, kOutPix = COUT * 2;  // bytes per pixel = one swizzle row
+    static constexpr uint32_t kSwIn = CIN == 64 ? 2 : (CIN == 32 ? 4 : 6);
+    static constexpr uint32_t kSwOut = COUT == 64 ? 2 : (COUT == 32 ? 4 : 6);
+    static constexpr int kInCopy = kSlab * kInPix, kInRow = (kInCopy + 1023) / 1024 * 1024;
+    static constexpr int kOutCopy = kTileM * kOutPix, kOutRow = (kOutCopy + 1023) / 1024 * 1024;
+    static constexpr int kTaps = 128 / CIN;                // taps per M tile
+    static constexpr int kMT = (3 + kTaps - 1) / kTaps;    // M tiles per row offset
+    static constexpr int kAcc = 3 * kMT;                   // accumulators of COUT columns
+    static constexpr int kIn = 0;
+    static constexpr int kOut = kIn + RING * kInRow;
+    // Operand reads of the dropped taps run up to 8 pixels past a row
+    // buffer's copy; every buffer is padded to 136 pixels or more, and 4 KB
+    // of slack follow the last one.
+    static constexpr int kBars = kOut + RING * kOutRow + 4096;
+    static constexpr int kNumBars = 4 * RING + 1;  // in full / empty, out full / empty, done
+    static constexpr int kTmemSlot = kBars + kNumBars * 8;
+    static constexpr int kAbort = kTmemSlot + 4;
+    static constexpr int kBytes = kAbort + 4;
+    static constexpr uint32_t kCols = kAcc * COUT <= 32 ? 32 : (kAcc * COUT <= 64 ? 64 : (kAcc * COUT <= 128 ? 128 : 256));
+};
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// MN-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t instr_desc_bf16_mn(int n) {
+    return instr_desc_bf16(n) | (1u << 15) | (1u << 16);
+}
+
+template <int CIN, int COUT, int RING>
+__global__ void __launch_bounds__(kThreadsTc, 2)
+    k_conv_wgrad_tc(const __grid_constant__ CUtensorMap in_map, const __grid_constant__ CUtensorMap out_map,
+                    const WgradParams p) {
+    using Lay = WgLayout<CIN, COUT, RING>;
+    static_assert((CIN == 16 || CIN == 32 || CIN == 64) && (COUT == 16 || COUT == 32 || COUT == 64), "shape");
+    extern __shared__ __align__(1024) unsigned char sm[];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sm + Lay::kBars);
+    uint64_t *in_full = bars, *in_empty = bars + RING, *out_full = bars + 2 * RING, *out_empty = bars + 3 * RING,
+             *done = bars + 4 * RING;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + Lay::kTmemSlot);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(sm + Lay::kAbort);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < RING; ++i) {
+            mbar_init(&in_full[i], 1);
+            mbar_init(&in_empty[i], 1);
+            mbar_init(&out_full[i], 1);
+            mbar_init(&out_empty[i], 1);
+        }
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        fence_barrier_init();
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                     "r"(Lay::kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    if (smem_addr(sm) & 1023u) {
+        if (threadIdx.x == 0 && p.status) atomicOr(p.status, DEV_ERR_BOUNDS);
+        *abort_flag = 1;
+    }
+    __syncthreads();
+    // Items as in the forward pass: a 128-pixel band of one image, a chunk of
+    // its rows.
+    ConvTcParams ip{};
+    ip.n = p.n;
+    ip.h = p.h;
+    ip.w = p.w;
+    ip.bands = p.bands;
+    ip.chunks = p.chunks;
+    ip.rows_per_chunk = p.rows_per_chunk;
+
+    if (warp == kCopyWarp) {
+        if (lane == 0) {
+            uint32_t li = 0, lo = 0;  // input rows, output-gradient rows issued
+            auto in_row = [&](int r, const Item &t) {
+                const int slot = (int)(li % RING);
+                if (!mbar_wait_bounded(&in_empty[slot], ((li / RING) & 1u) ^ 1u, p.status)) return false;
+                mbar_arrive_expect_tx(&in_full[slot], Lay::kInCopy);
+                tma_load_row(smem_addr(sm + Lay::kIn + slot * Lay::kInRow), &in_map, t.x0 - 1, r, t.img, &in_full[slot]);
+                ++li;
+                return true;
+            };
+            auto out_row = [&](int r, const Item &t) {
+                const int slot = (int)(lo % RING);
+                if (!mbar_wait_bounded(&out_empty[slot], ((lo / RING) & 1u) ^ 1u, p.status)) return false;
+                mbar_arrive_expect_tx(&out_full[slot], Lay::kOutCopy);
+                tma_load_row(smem_addr(sm + Lay::kOut + slot * Lay::kOutRow), &out_map, t.x0, r, t.img, &out_full[slot]);
+                ++lo;
+                return true;
+            };
+            bool ok = true;
+            for (int it = blockIdx.x; it < p.items && ok && !*abort_flag; it += gridDim.x) {
+                const Item t = item_of(ip, it);
+                ok = in_row(t.y0 - 1, t) && in_row(t.y0, t);
+                for (int j = 0; j < t.rows && ok; ++j) ok = in_row(t.y0 + j + 1, t) && out_row(t.y0 + j, t);
+            }
+            if (!ok) *abort_flag = 1;
+            for (uint32_t q = li > RING ? li - RING : 0; q < li; ++q)
+                mbar_wait_bounded(&in_full[q % RING], (q / RING) & 1u, nullptr);
+            for (uint32_t q = lo > RING ? lo - RING : 0; q < lo; ++q)
+                mbar_wait_bounded(&out_full[q % RING], (q / RING) & 1u, nullptr);
+        }
+        __syncwarp();
+    } else if (warp == kMmaWarp) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = instr_desc_bf16_mn(COUT);
+            const uint32_t ibase = smem_addr(sm + Lay::kIn), obase = smem_addr(sm + Lay::kOut);
+            uint32_t li = 0, lo = 0;
+            bool ok = true, fresh = true;
+            for (int it = blockIdx.x; it < p.items && ok && !*abort_flag; it += gridDim.x) {
+                const Item t = item_of(ip, it);
+                const uint32_t base = li;
+                for (int j = 0; j < t.rows && ok; ++j, ++lo) {
+                    // Input rows y - 1, y, y + 1 of output-gradient row y = y0 + j.
+                    for (uint32_t q = j == 0 ? base : base + j + 2; q <= base + j + 2 && ok; ++q)
+                        ok = mbar_wait_bounded(&in_full[q % RING], (q / RING) & 1u, p.status);
+                    if (ok) ok = mbar_wait_bounded(&out_full[lo % RING], (lo / RING) & 1u, p.status);
+                    if (!ok) break;
+                    tc_fence_after();
+                    const uint64_t b0 = smem_desc(obase + (lo % RING) * Lay::kOutRow, 16, 8 * Lay::kOutPix, Lay::kSwOut);
+#pragma unroll
+                    for (int dy = 0; dy < 3; ++dy) {
+                        const uint64_t a0 = smem_desc(ibase + ((base + j + dy) % RING) * Lay::kInRow, Lay::kInPix,
+                                                      8 * Lay::kInPix, Lay::kSwIn);
+#pragma unroll
+                        for (int mt = 0; mt < Lay::kMT; ++mt)
+#pragma unroll
+                            for (int ks = 0; ks < kTileM / 16; ++ks) {
+                                // Offsets in 16-byte units: tap block mt starts
+                                // mt * kTaps pixels in, K step ks 16 pixels on.
+                                const uint64_t ao = (uint64_t)((mt * Lay::kTaps + 16 * ks) * Lay::kInPix >> 4);
+                                const uint64_t bo = (uint64_t)(16 * ks * Lay::kOutPix >> 4);
+                                umma_bf16(tmem + (dy * Lay::kMT + mt) * COUT, a0 + ao, b0 + bo, idesc,
+                                          fresh && ks == 0 ? 0u : 1u);
+                            }
+                    }
+                    fresh = false;
+                    umma_commit(&out_empty[lo % RING]);
+                    umma_commit(&in_empty[(base + j) % RING]);
+                    if (j == t.rows - 1) {
+                        umma_commit(&in_empty[(base + j + 1) % RING]);
+                        umma_commit(&in_empty[(base + j + 2) % RING]);
+                    }
+                }
+                li = base + t.rows + 2;
+            }
+            if (!ok) *abort_flag = 1;
+            umma_commit(done);
+        }
+        __syncwarp();
+    } else {
+        // Epilogue, once: accumulator (dy, mt), lane m = 32 * warp + lane is
+        // tap dx = mt * kTaps + m / CIN, channel m % CIN.
+        const bool ok = __all_sync(~0u, mbar_wait_bounded(done, 0, p.status));
+        if (ok && !__any_sync(~0u, *abort_flag)) {
+            tc_fence_after();
+            const int m = warp * 32 + lane, ci = m % CIN;
+            float *part = p.partials + (size_t)blockIdx.x * COUT * 9 * CIN;
+#pragma unroll 1
+            for (int a = 0; a < Lay::kAcc; ++a) {
+                const int dy = a / Lay::kMT, dx = (a % Lay::kMT) * Lay::kTaps + m / CIN;
+                float v[COUT];
+#pragma unroll
+                for (int c = 0; c < COUT; c += 16)
+                    tmem_load16(tmem + ((uint32_t)(warp * 32) << 16) + a * COUT + c, v + c);
+                if (dx < 3) {
+#pragma unroll
+                    for (int co = 0; co < COUT; ++co) part[((size_t)co * 9 + dy * 3 + dx) * CIN + ci] = v[co];
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Lay::kCols) : "memory");
+    }
+}
+
+// Rows map over an NHWC BF16 tensor (channels, x, row, image), box of `box_px`
+// pixels, swizzled by a pixel's bytes (C = 16, 32 or 64).
+bool encode_rows_map(CUtensorMap *map, const void *base, int C, int n, int h, int w, int box_px) {
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode) return false;
+    const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
+    const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)w * C * 2, (cuuint64_t)h * w * C * 2};
+    const cuuint32_t box[4] = {(cuuint32_t)C, (cuuint32_t)box_px, 1, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUtensorMapSwizzle swz =
+        C == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : (C == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B);
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// CTA slots of a kernel with `smem` bytes of shared memory: two per SM at most.
+cudaError_t cta_slots(int smem, int *slots) {
+    int dev = 0, sms = 0, smem_sm = 0, reserved = 0;
+    cudaError_t e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess)
+        return e;
+    if ((e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess)
+        return e;
+    int per_sm = smem_sm / (smem + reserved);
+    per_sm = per_sm < 1 ? 1 : (per_sm > 2 ? 2 : per_sm);
+    *slots = sms * per_sm;
+    return cudaSuccess;
+}
+
+template <int CIN, int COUT>
+cudaError_t launch_wgrad_tc(const __nv_bfloat16 *dout, const __nv_bfloat16 *in, WgradParams p, int max_parts,
+                            int *parts, cudaStream_t s) {
+    constexpr int kBudget = 113 * 1024;
+    constexpr int kFixed = WgLayout<CIN, COUT, 8>::kBytes - 8 * (WgLayout<CIN, COUT, 8>::kInRow + WgLayout<CIN, COUT, 8>::kOutRow);
+    constexpr int kFit = (kBudget - kFixed) / (WgLayout<CIN, COUT, 8>::kInRow + WgLayout<CIN, COUT, 8>::kOutRow);
+    constexpr int RING = kFit < 3 ? 3 : (kFit > 8 ? 8 : kFit);
+    using Lay = WgLayout<CIN, COUT, RING>;
+    constexpr int kSmem = Lay::kBytes < 80 * 1024 ? 80 * 1024 : Lay::kBytes;
+    auto kern = k_conv_wgrad_tc<CIN, COUT, RING>;
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [&] {
+        attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
+        if (attr_err == cudaSuccess)
+            attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                            (int)cudaSharedmemCarveoutMaxShared);
+    });
+    if (attr_err != cudaSuccess) return attr_err;
+    alignas(64) CUtensorMap in_map, out_map;
+    if (!encode_rows_map(&in_map, in, CIN, p.n, p.h, p.w, kSlab) ||
+        !encode_rows_map(&out_map, dout, COUT, p.n, p.h, p.w, kTileM))
+        return cudaErrorInvalidValue;
+    int slots = 0;
+    cudaError_t e = cta_slots(kSmem, &slots);
+    if (e != cudaSuccess) return e;
+    if (slots > max_parts) slots = max_parts;
+    p.bands = (p.w + kTileM - 1) / kTileM;
+    const long long strips = (long long)p.n * p.bands;
+    long long rpc = (strips * p.h + slots - 1) / slots;
+    if (rpc < 4) rpc = 4;
+    if (rpc > p.h) rpc = p.h;
+    p.rows_per_chunk = (int)rpc;
+    p.chunks = (p.h + p.rows_per_chunk - 1) / p.rows_per_chunk;
+    const long long items = strips * p.chunks;
+    if (items > 0x7fffffffLL || slots < 1) return cudaErrorInvalidValue;
+    p.items = (int)items;
+    const int grid = p.items < slots ? p.items : slots;
+    kern<<<grid, kThreadsTc, kSmem, s>>>(in_map, out_map, p);
+    *parts = grid;
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 // 3x3 convolution of NHWC BF16 input with weights [COUT][9][CIN] on the
@@ -508,6 +789,30 @@ cudaError_t conv_fwd_tc(int cin, int cout, bool relu, bool out_f32, const __nv_b
     GINF_TC_CASE(32, 16)
     GINF_TC_CASE(32, 64)
 #undef GINF_TC_CASE
+    return cudaErrorInvalidValue;
+}
+
+// Weight gradient of the 3x3 convolution on the tcgen05 path: per-CTA
+// partial sums [parts][COUT][9][CIN] into `partials` (room for max_parts),
+// their count in *parts; cudaErrorInvalidValue for a channel pair it is not
+// built for.
+cudaError_t conv_wgrad_tc(int cin, int cout, const __nv_bfloat16 *dout, const __nv_bfloat16 *in, int nimg, int h,
+                          int wd, float *partials, int max_parts, int *parts, int *status, cudaStream_t s) {
+    if (((uintptr_t)dout | (uintptr_t)in) & 15) return cudaErrorMisalignedAddress;
+    WgradParams p{};
+    p.partials = partials;
+    p.n = nimg;
+    p.h = h;
+    p.w = wd;
+    p.status = status;
+#define GINF_WG_TC_CASE(CI, CO) \
+    if (cin == CI && cout == CO) return launch_wgrad_tc<CI, CO>(dout, in, p, max_parts, parts, s);
+    GINF_WG_TC_CASE(16, 32)
+    GINF_WG_TC_CASE(32, 32)
+    GINF_WG_TC_CASE(64, 32)
+    GINF_WG_TC_CASE(32, 16)
+    GINF_WG_TC_CASE(32, 64)
+#undef GINF_WG_TC_CASE
     return cudaErrorInvalidValue;
 }
 

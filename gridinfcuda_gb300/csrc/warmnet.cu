@@ -1,10 +1,10 @@
 // warmnet.cu -- the learned warm start: a small convolutional network that
 // maps the costs of a pyramid level to the messages its nodes should start
 // from (on the beliefs' scale), with
-// hand-written tensor-core kernels -- the forward and data-gradient
-// convolutions on tcgen05 with tensor-memory accumulators (conv_tc.cu), the
-// weight gradient on mma.sync m16n8k16 (BF16, FP32 accumulate) -- the loss,
-// ReLU, bias-gradient and Adam kernels, and a checkpoint format.
+// hand-written tensor-core kernels -- the forward, data-gradient and
+// weight-gradient convolutions on tcgen05 with tensor-memory accumulators
+// (conv_tc.cu) -- the loss, ReLU, bias-gradient and Adam kernels, and a
+// checkpoint format.
 //
 // Network (L labels, h hidden channels): conv3x3(L->h) ReLU, conv3x3(h->h)
 // ReLU, conv3x3(h->h) ReLU, conv3x3(h->L); zero padding; activations NHWC.
@@ -31,6 +31,8 @@ namespace ginf_gpu {
 cudaError_t conv_fwd_tc(int cin, int cout, bool relu, bool out_f32, const __nv_bfloat16 *in, const __nv_bfloat16 *w,
                         const float *bias, int nimg, int h, int wd, void *out, const float *res, int *status,
                         cudaStream_t s);
+cudaError_t conv_wgrad_tc(int cin, int cout, const __nv_bfloat16 *dout, const __nv_bfloat16 *in, int nimg, int h,
+                          int wd, float *partials, int max_parts, int *parts, int *status, cudaStream_t s);
 
 namespace {
 
@@ -42,72 +44,14 @@ __device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo, __nv_bfloat16 hi
     return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
 }
 
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
 
 struct Geo {
     int n, h, w;  // images, rows, columns
 };
 
-// Weight gradient: dW[co][tap][ci] = sum over pixels of dout[p][co] *
-// in[p shifted by tap][ci], as GEMM M = COUT, N = 9*CIN, K = pixels.  Block
-// (chunk of kChunk pixels) x (4 warps, one 16x8 output tile each); partial
-// sums per chunk, added in a fixed order by k_reduce_partials.
+// Pixels per bias-gradient partial sum, added in a fixed order by
+// k_reduce_partials.
 constexpr int kChunk = 1024;
-
-template <int CIN, int COUT>
-__global__ void __launch_bounds__(128) k_conv_wgrad(const __nv_bfloat16 *__restrict__ dout,
-                                                    const __nv_bfloat16 *__restrict__ in, Geo g,
-                                                    float *__restrict__ partials) {
-    constexpr int NT = 9 * CIN / 8;  // n tiles
-    constexpr int TILES = COUT / 16 * NT;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int gid = lane >> 2, tig = lane & 3;
-    const int tile = blockIdx.y * 4 + warp;
-    if (tile >= TILES) return;
-    const int mt = tile / NT, nt = tile % NT;
-    const int co_a = mt * 16 + gid, co_b = co_a + 8;
-    const int kcol = nt * 8 + gid;  // this lane's B column
-    const int tap = kcol / CIN, ci = kcol % CIN;
-    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-    const int npix = g.n * g.h * g.w;
-    const int pbeg = blockIdx.x * kChunk, pend = min(npix, pbeg + kChunk);
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
-    auto dv = [&](int p, int co) -> __nv_bfloat16 {
-        return p < pend ? dout[(size_t)p * COUT + co] : __float2bfloat16_rn(0.f);
-    };
-    auto iv = [&](int p) -> __nv_bfloat16 {
-        if (p >= pend) return __float2bfloat16_rn(0.f);
-        const int x = p % g.w, t = p / g.w, y = t % g.h, n = t / g.h;
-        const int yy = y + dy, xx = x + dx;
-        if (yy < 0 || yy >= g.h || xx < 0 || xx >= g.w) return __float2bfloat16_rn(0.f);
-        return in[((size_t)(n * g.h + yy) * g.w + xx) * CIN + ci];
-    };
-#pragma unroll 1
-    for (int k0 = pbeg; k0 < pend; k0 += 16) {
-        const int q = k0 + tig * 2;
-        uint32_t a[4], b[2];
-        a[0] = pack_bf16(dv(q, co_a), dv(q + 1, co_a));
-        a[1] = pack_bf16(dv(q, co_b), dv(q + 1, co_b));
-        a[2] = pack_bf16(dv(q + 8, co_a), dv(q + 9, co_a));
-        a[3] = pack_bf16(dv(q + 8, co_b), dv(q + 9, co_b));
-        b[0] = pack_bf16(iv(q), iv(q + 1));
-        b[1] = pack_bf16(iv(q + 8), iv(q + 9));
-        mma_bf16(acc, a, b);
-    }
-    // acc: rows co_a / co_b, columns nt*8 + tig*2 + {0,1}
-    float *part = partials + (size_t)blockIdx.x * COUT * 9 * CIN;
-    const int col = nt * 8 + tig * 2;
-    part[(size_t)co_a * 9 * CIN + col] = acc[0];
-    part[(size_t)co_a * 9 * CIN + col + 1] = acc[1];
-    part[(size_t)co_b * 9 * CIN + col] = acc[2];
-    part[(size_t)co_b * 9 * CIN + col + 1] = acc[3];
-}
 
 // Bias gradient partials: sum over a chunk of pixels of g[p][c] (FP32).
 __global__ void k_bias_partials(const float *__restrict__ g, int npix, int C, float *__restrict__ partials) {
@@ -232,20 +176,6 @@ uint64_t fnv1a(const void *data, size_t n, uint64_t h = 1469598103934665603ull) 
 
 }  // namespace
 
-// Weight-gradient instantiations for the channel counts the network uses
-// (L in {16, 32, 64}, 32 hidden channels).
-template <int CIN, int COUT>
-cudaError_t conv_wgrad_t(const __nv_bfloat16 *dout, const __nv_bfloat16 *in, Geo g, float *partials, float *dw,
-                         cudaStream_t s) {
-    const int npix = g.n * g.h * g.w;
-    const int chunks = (npix + kChunk - 1) / kChunk;
-    constexpr int TILES = COUT / 16 * (9 * CIN / 8);
-    k_conv_wgrad<CIN, COUT><<<dim3(chunks, (TILES + 3) / 4), 128, 0, s>>>(dout, in, g, partials);
-    const int n = COUT * 9 * CIN;
-    k_reduce_partials<<<nblocks(n), kThreads, 0, s>>>(partials, chunks, n, dw);
-    return cudaGetLastError();
-}
-
 }  // namespace ginf_gpu
 
 using namespace ginf_gpu;
@@ -360,10 +290,13 @@ ginf_status ensure_batch(ginf_warmnet *n, size_t pix) {
     GINF_WCK(cudaMalloc(&n->gtmp, pix * cmax * sizeof(float)));
     GINF_WCK(cudaMalloc(&n->gb, pix * cmax * sizeof(__nv_bfloat16)));
     n->cap_pix = pix;
+    // Partial sums: one per bias chunk of pixels, and one per CTA of the
+    // weight gradient (up to two per SM).
     const size_t chunks = (pix + kChunk - 1) / kChunk;
-    size_t need = 0;
-    for (int l = 0; l < 4; ++l) need = std::max(need, chunks * (size_t)n->cout[l] * 9 * n->cin[l]);
-    need = std::max(need, chunks * cmax);
+    int sms = 0;
+    GINF_WCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, n->device));
+    size_t need = chunks * cmax;
+    for (int l = 0; l < 4; ++l) need = std::max(need, (size_t)2 * sms * n->cout[l] * 9 * n->cin[l]);
     if (need > n->cap_partials) {
         cudaFree(n->partials);
         GINF_WCK(cudaMalloc(&n->partials, need * sizeof(float)));
@@ -378,17 +311,18 @@ cudaError_t conv_fwd(int cin, int cout, bool relu, bool out_f32, const __nv_bflo
     return conv_fwd_tc(cin, cout, relu, out_f32, in, w, bias, g.n, g.h, g.w, out, res, status, s);
 }
 
+// Weight gradient on the tcgen05 path: per-CTA partial sums, then their sum
+// in CTA order (deterministic).
 cudaError_t conv_wgrad(int cin, int cout, const __nv_bfloat16 *dout, const __nv_bfloat16 *in, Geo g, float *part,
-                       float *dw, cudaStream_t s) {
-#define GINF_WG_CASE(CI, CO) \
-    if (cin == CI && cout == CO) return conv_wgrad_t<CI, CO>(dout, in, g, part, dw, s);
-    GINF_WG_CASE(16, 32)
-    GINF_WG_CASE(32, 32)
-    GINF_WG_CASE(64, 32)
-    GINF_WG_CASE(32, 16)
-    GINF_WG_CASE(32, 64)
-#undef GINF_WG_CASE
-    return cudaErrorInvalidValue;
+                       size_t part_cap, float *dw, int *status, cudaStream_t s) {
+    const size_t nw = (size_t)cout * 9 * cin;
+    const size_t cap = part_cap / nw;
+    int parts = 0;
+    cudaError_t e = conv_wgrad_tc(cin, cout, dout, in, g.n, g.h, g.w, part, cap > 0x7fffffff ? 0x7fffffff : (int)cap,
+                                  &parts, status, s);
+    if (e != cudaSuccess) return e;
+    k_reduce_partials<<<nblocks(nw), kThreads, 0, s>>>(part, parts, (int)nw, dw);
+    return cudaGetLastError();
 }
 
 // y = x + net(x) into y_out (the network's own buffer when null); the last
@@ -427,7 +361,8 @@ ginf_status backward(ginf_warmnet *n, const float *target, Geo g, cudaStream_t s
         k_reduce_partials<<<nblocks(co), kThreads, 0, s>>>(n->partials, chunks, co, n->grads + n->boff[l]);
         GINF_WCK(cudaGetLastError());
         // weight gradient
-        GINF_WCK(conv_wgrad(ci, co, n->gb, n->a[l], g, n->partials, n->grads + n->woff[l], s));
+        GINF_WCK(conv_wgrad(ci, co, n->gb, n->a[l], g, n->partials, n->cap_partials, n->grads + n->woff[l], n->status,
+                            s));
         if (l == 0) break;
         // data gradient: conv of the (BF16) output gradient with the flipped weights
         k_flip_weights<<<nblocks((size_t)ci * 9 * co), kThreads, 0, s>>>(n->wbf + n->woff[l], ci, co, n->wflip);
