@@ -63,12 +63,21 @@ __global__ void k_bias_partials(const float *__restrict__ g, int npix, int C, fl
     partials[(size_t)blockIdx.x * C + c] = s;
 }
 
-// out[i] = sum over chunks k of partials[k][i], in chunk order.
+// out[i] = sum over chunks k of partials[k][i], in chunk order; eight
+// partials loaded ahead of their additions.
 __global__ void k_reduce_partials(const float *__restrict__ partials, int chunks, int n, float *__restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float s = 0.f;
-    for (int k = 0; k < chunks; ++k) s += partials[(size_t)k * n + i];
+    int k = 0;
+    for (; k + 8 <= chunks; k += 8) {
+        float v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = partials[(size_t)(k + j) * n + i];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) s += v[j];
+    }
+    for (; k < chunks; ++k) s += partials[(size_t)k * n + i];
     out[i] = s;
 }
 
@@ -134,11 +143,34 @@ __global__ void k_sum_double(const double *p, int n, double denom, float *out) {
 // g = grad of a ReLU output times (activation > 0), FP32 and a BF16 copy.
 __global__ void k_relu_bwd(const float *__restrict__ grad, const __nv_bfloat16 *__restrict__ act, size_t n,
                            float *__restrict__ g, __nv_bfloat16 *__restrict__ gb) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float v = __bfloat162float(act[i]) > 0.f ? grad[i] : 0.f;
-    g[i] = v;
-    gb[i] = __float2bfloat16_rn(v);
+    // Eight values per thread (16-byte accesses) when every buffer is
+    // 16-byte aligned, grid-stride, scalar tail.
+    const size_t n8 = (((uintptr_t)grad | (uintptr_t)act | (uintptr_t)g | (uintptr_t)gb) & 15) == 0 ? n / 8 : 0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (size_t i = t; i < n8; i += stride) {
+        const float4 g0 = reinterpret_cast<const float4 *>(grad)[2 * i], g1 = reinterpret_cast<const float4 *>(grad)[2 * i + 1];
+        const uint4 a = reinterpret_cast<const uint4 *>(act)[i];
+        const float gv[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
+        const uint32_t aw[4] = {a.x, a.y, a.z, a.w};
+        float o[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const uint16_t bits = (uint16_t)(aw[j / 2] >> (16 * (j & 1)));
+            o[j] = __bfloat162float(__ushort_as_bfloat16(bits)) > 0.f ? gv[j] : 0.f;
+        }
+        reinterpret_cast<float4 *>(g)[2 * i] = make_float4(o[0], o[1], o[2], o[3]);
+        reinterpret_cast<float4 *>(g)[2 * i + 1] = make_float4(o[4], o[5], o[6], o[7]);
+        reinterpret_cast<uint4 *>(gb)[i] = make_uint4(pack_bf16(__float2bfloat16_rn(o[0]), __float2bfloat16_rn(o[1])),
+                                                      pack_bf16(__float2bfloat16_rn(o[2]), __float2bfloat16_rn(o[3])),
+                                                      pack_bf16(__float2bfloat16_rn(o[4]), __float2bfloat16_rn(o[5])),
+                                                      pack_bf16(__float2bfloat16_rn(o[6]), __float2bfloat16_rn(o[7])));
+    }
+    for (size_t i = n8 * 8 + t; i < n; i += stride) {
+        const float v = __bfloat162float(act[i]) > 0.f ? grad[i] : 0.f;
+        g[i] = v;
+        gb[i] = __float2bfloat16_rn(v);
+    }
 }
 
 // Adam (bias-corrected) on FP32 master weights, refreshing the BF16 copy.
@@ -369,7 +401,8 @@ ginf_status backward(ginf_warmnet *n, const float *target, Geo g, cudaStream_t s
         GINF_WCK(cudaGetLastError());
         GINF_WCK(conv_fwd(co, ci, false, true, n->gb, n->wflip, nullptr, g, n->gtmp, nullptr, n->status, s));
         // through the ReLU of layer l-1's output
-        k_relu_bwd<<<nblocks(pix * ci), kThreads, 0, s>>>(n->gtmp, n->a[l], pix * ci, n->g32, n->gb);
+        k_relu_bwd<<<(unsigned)std::min<size_t>(4096, std::max<size_t>(1, nblocks(pix * ci / 8))), kThreads, 0, s>>>(
+            n->gtmp, n->a[l], pix * ci, n->g32, n->gb);
         GINF_WCK(cudaGetLastError());
         gl = n->g32;
     }
