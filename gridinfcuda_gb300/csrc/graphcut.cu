@@ -92,6 +92,9 @@ __device__ void active_diagonals(const AlphaBetaParams &p, Shared &sh) {
     __syncthreads();
 }
 
+// Barrier 1 over the block's first `n` threads (a multiple of 32).
+__device__ __forceinline__ void bar_sync_first(int n) { asm volatile("bar.sync 1, %0;" ::"r"(n) : "memory"); }
+
 // Sum of v over the block, in int32 (wrapping, as the reference's int sums).
 __device__ int block_sum(int v, Shared &sh) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -177,6 +180,10 @@ __global__ void __launch_bounds__(kThreadsAB, 1) k_alpha_beta(const AlphaBetaPar
     const int32_t NP2 = (int32_t)N + 2;
     int32_t *f = p.result, *nf = p.newr, *ex = p.excess, *ht = p.height, *res = p.res;
     const uint64_t t0 = global_timer_ns();
+    // Threads taking part in the wavefronts: enough whole warps for the
+    // longest diagonal, min(W, H) nodes.
+    const int mwh = W < H ? W : H;
+    const int nwave = mwh >= (int)blockDim.x ? (int)blockDim.x : (mwh + 31) / 32 * 32;
     // result and newResult start as the initial labelling (graphcut.cc:205, 215).
     for (size_t i = threadIdx.x; i < N; i += blockDim.x) nf[i] = f[i];
     const int c0 = energy_i32(p, f, sh);
@@ -246,12 +253,15 @@ __global__ void __launch_bounds__(kThreadsAB, 1) k_alpha_beta(const AlphaBetaPar
                         // and are left out.
                         active_diagonals(p, sh);
                         if (sh.kmin > sh.kmax) break;
-                        // Pushes (graphcut.cc:143-177), raster order as wavefronts.
+                        // Pushes (graphcut.cc:143-177), raster order as wavefronts,
+                        // on the warps that can hold a diagonal's nodes; the
+                        // others wait at the end of the sweep.
+                        if ((int)threadIdx.x < nwave)
                         for (int k = sh.kmin; k <= sh.kmax; ++k) {
                             if (!diag_visit(sh, k, bits)) continue;
                             const int xlo = k - (H - 1) > 0 ? k - (H - 1) : 0;
                             const int xhi = k < W - 1 ? k : W - 1;
-                            for (int x = xlo + (int)threadIdx.x; x <= xhi; x += blockDim.x) {
+                            for (int x = xlo + (int)threadIdx.x; x <= xhi; x += nwave) {
                                 const int y = k - x;
                                 const size_t i = (size_t)y * W + x;
                                 // Everything this push reads, loaded at once: no
@@ -296,17 +306,19 @@ __global__ void __launch_bounds__(kThreadsAB, 1) k_alpha_beta(const AlphaBetaPar
                                 }
                                 ex[i] = e;
                             }
-                            __syncthreads();
+                            bar_sync_first(nwave);
                         }
+                        __syncthreads();
                         // Relabels (graphcut.cc:180-195), raster order as
                         // wavefronts: they change only active nodes' heights and
                         // no excess, so the active diagonals bound them.
                         active_diagonals(p, sh);
+                        if ((int)threadIdx.x < nwave)
                         for (int k = sh.kmin; k <= sh.kmax; ++k) {
                             if (!diag_visit(sh, k, bits)) continue;
                             const int xlo = k - (H - 1) > 0 ? k - (H - 1) : 0;
                             const int xhi = k < W - 1 ? k : W - 1;
-                            for (int x = xlo + (int)threadIdx.x; x <= xhi; x += blockDim.x) {
+                            for (int x = xlo + (int)threadIdx.x; x <= xhi; x += nwave) {
                                 const int y = k - x;
                                 const size_t i = (size_t)y * W + x;
                                 // Loaded at once: the west and north neighbours'
@@ -331,8 +343,9 @@ __global__ void __launch_bounds__(kThreadsAB, 1) k_alpha_beta(const AlphaBetaPar
                                     ht[i] = mh + 1;
                                 }
                             }
-                            __syncthreads();
+                            bar_sync_first(nwave);
                         }
+                        __syncthreads();
                     }
                 }
                 if (sh.stop) break;
