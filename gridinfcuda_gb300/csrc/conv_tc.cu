@@ -19,22 +19,31 @@
 // operand of tap (dy, dx) is the buffer of row y + dy read from pixel dx + 1
 // on, a descriptor whose start is one swizzle row further per pixel -- the
 // nine taps are nine descriptors over three row buffers, nothing is copied
-// per tap.  The weights, [tap][8-channel chunk][co][8] in the canonical
-// layout without swizzle, stay in shared memory for the CTA's life.
+// per tap.
+//
+// The weights, [dx][8-channel chunk][j * COUT + co][8] in the canonical
+// layout without swizzle, stack the three row offsets dy = j - 1 along N, so
+// one MMA (N = 3 * COUT) applies an input row r to the accumulators of output
+// rows r + 1, r and r - 1 at once; those live in a descending ring of
+// tensor-memory slots (adjacent unless the ring wraps, when the run splits in
+// two), and the first block into a fresh slot overwrites it.
 //
 // Roles (192 threads): warp 4 lane 0 issues the row copies into a ring of
-// RING buffers; warp 5 lane 0 issues the 9 * CIN / 16 MMAs of a tile into one
-// of two tensor-memory accumulators and commits them to mbarriers (the
-// accumulator is full, and a row buffer whose last tile is done is free);
-// warps 0-3 read the accumulator back (warp w owns lanes 32w..32w+31, i.e.
-// pixels 32w.. of the tile), add the bias, apply ReLU and the residual, and
-// store.  Every wait is bounded (DEV_ERR_TIMEOUT in the status word), and
-// the tensor memory is released on every path.
+// RING buffers; warp 5 lane 0 issues, per input row, 3 * CIN / 16 steps of
+// one or two MMAs (descriptors formed once per row, compile-time step
+// offsets) and commits them to mbarriers (a row buffer is free after its own
+// MMAs; an output row's accumulator is full after input row r + 1); warps 0-3
+// read the accumulator back (warp w owns lanes 32w..32w+31, i.e. pixels 32w..
+// of the tile), add the bias, apply ReLU, stage the warp's 32 pixels in
+// shared memory and store them 512 bytes per instruction, adding the
+// residual in that pass.  Every wait is bounded (DEV_ERR_TIMEOUT in the
+// status word), and the tensor memory is released on every path.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "ginf_internal.h"
@@ -396,6 +405,25 @@ __global__ void __launch_bounds__(kThreadsTc, 2)
     }
 }
 
+// Per device, once: the kernel's dynamic shared-memory limit and a
+// preference for the largest shared-memory split (without it the driver may
+// pick a split that holds one of these CTAs per SM, not two).
+struct TcKernelSetup {
+    SmemLimit smem;
+    std::atomic<bool> carveout[kMaxDevices];
+    template <typename K>
+    cudaError_t ensure(K kern, int bytes) {
+        cudaError_t e = smem.ensure(kern, (size_t)bytes);
+        if (e != cudaSuccess) return e;
+        std::atomic<bool> &c = carveout[current_device()];
+        if (c.load(std::memory_order_acquire)) return cudaSuccess;
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+        if (e == cudaSuccess) c.store(true, std::memory_order_release);
+        return e;
+    }
+};
+
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     static std::once_flag once;
@@ -424,16 +452,8 @@ cudaError_t launch_conv_tc(const __nv_bfloat16 *in, ConvTcParams p, cudaStream_t
     // tensor-memory columns (a third would wait in its allocation).
     constexpr int kSmem = Lay::kBytes < 80 * 1024 ? 80 * 1024 : Lay::kBytes;
     auto kern = k_conv_tc<CIN, COUT, RELU, OUT_F32, RING>;
-    static std::once_flag once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(once, [&] {
-        attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
-        // Without a carveout preference the occupancy query assumes a smaller
-        // shared-memory split and sizes the grid for one CTA per SM.
-        if (attr_err == cudaSuccess)
-            attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                            (int)cudaSharedmemCarveoutMaxShared);
-    });
+    static TcKernelSetup setup;
+    cudaError_t attr_err = setup.ensure(kern, kSmem);
     if (attr_err != cudaSuccess) return attr_err;
     PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
     if (!encode) return cudaErrorNotSupported;
@@ -727,14 +747,8 @@ cudaError_t launch_wgrad_tc(const __nv_bfloat16 *dout, const __nv_bfloat16 *in, 
     using Lay = WgLayout<CIN, COUT, RING>;
     constexpr int kSmem = Lay::kBytes < 80 * 1024 ? 80 * 1024 : Lay::kBytes;
     auto kern = k_conv_wgrad_tc<CIN, COUT, RING>;
-    static std::once_flag once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(once, [&] {
-        attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
-        if (attr_err == cudaSuccess)
-            attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                            (int)cudaSharedmemCarveoutMaxShared);
-    });
+    static TcKernelSetup setup;
+    cudaError_t attr_err = setup.ensure(kern, kSmem);
     if (attr_err != cudaSuccess) return attr_err;
     alignas(64) CUtensorMap in_map, out_map;
     if (!encode_rows_map(&in_map, in, CIN, p.n, p.h, p.w, kSlab) ||
