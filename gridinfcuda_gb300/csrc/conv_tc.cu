@@ -439,6 +439,60 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     return fn;
 }
 
+// Rows map over an NHWC BF16 tensor (channels, x, row, image), box of `box_px`
+// pixels, swizzled by a pixel's bytes (C = 16, 32 or 64).
+bool encode_rows_map(CUtensorMap *map, const void *base, int C, int n, int h, int w, int box_px) {
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode) return false;
+    const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
+    const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)w * C * 2, (cuuint64_t)h * w * C * 2};
+    const cuuint32_t box[4] = {(cuuint32_t)C, (cuuint32_t)box_px, 1, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUtensorMapSwizzle swz =
+        C == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : (C == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B);
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// CTA slots of a kernel with `smem` bytes of shared memory: two per SM at most.
+cudaError_t cta_slots(int smem, int *slots) {
+    int dev = 0, sms = 0, smem_sm = 0, reserved = 0;
+    cudaError_t e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess)
+        return e;
+    if ((e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess)
+        return e;
+    int per_sm = smem_sm / (smem + reserved);
+    per_sm = per_sm < 1 ? 1 : (per_sm > 2 ? 2 : per_sm);
+    *slots = sms * per_sm;
+    return cudaSuccess;
+}
+
+// Work items for `slots` CTAs: each band's rows split into chunks so that the
+// items about fill the GPU once, at least four rows per chunk (two halo rows
+// per chunk).  False when there is nothing to do or too much to count.
+struct ItemPlan {
+    int bands, rows_per_chunk, chunks, items, grid;
+};
+
+bool plan_items(int n, int h, int w, int slots, ItemPlan &pl) {
+    if (n < 1 || h < 1 || w < 1 || slots < 1) return false;
+    pl.bands = (w + kTileM - 1) / kTileM;
+    const long long strips = (long long)n * pl.bands;
+    long long rpc = (strips * h + slots - 1) / slots;
+    rpc = rpc < 4 ? 4 : (rpc > h ? h : rpc);
+    pl.rows_per_chunk = (int)rpc;
+    pl.chunks = (h + pl.rows_per_chunk - 1) / pl.rows_per_chunk;
+    const long long items = strips * pl.chunks;
+    if (items > 0x7fffffffLL) return false;
+    pl.items = (int)items;
+    pl.grid = pl.items < slots ? pl.items : slots;
+    return true;
+}
+
 template <int CIN, int COUT, bool RELU, bool OUT_F32>
 cudaError_t launch_conv_tc(const __nv_bfloat16 *in, ConvTcParams p, cudaStream_t s) {
     // The deepest ring of row buffers (3 to 8) that leaves room for two CTAs
@@ -455,47 +509,19 @@ cudaError_t launch_conv_tc(const __nv_bfloat16 *in, ConvTcParams p, cudaStream_t
     static TcKernelSetup setup;
     cudaError_t attr_err = setup.ensure(kern, kSmem);
     if (attr_err != cudaSuccess) return attr_err;
-    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
-    if (!encode) return cudaErrorNotSupported;
-    // Rows map over the NHWC input (channels, x, row, image), swizzled by a pixel's bytes.
     alignas(64) CUtensorMap map;
-    const cuuint64_t dims[4] = {(cuuint64_t)CIN, (cuuint64_t)p.w, (cuuint64_t)p.h, (cuuint64_t)p.n};
-    const cuuint64_t strides[3] = {(cuuint64_t)CIN * 2, (cuuint64_t)p.w * CIN * 2, (cuuint64_t)p.h * p.w * CIN * 2};
-    const cuuint32_t box[4] = {(cuuint32_t)CIN, kSlab, 1, 1};
-    const cuuint32_t estr[4] = {1, 1, 1, 1};
-    const CUtensorMapSwizzle swz =
-        CIN == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : (CIN == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B);
-    if (encode(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16 *>(in), dims, strides, box, estr,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-        return cudaErrorInvalidValue;
-    int dev = 0, sms = 0, smem_sm = 0, reserved = 0;
-    cudaError_t e;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess)
-        return e;
-    if ((e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess)
-        return e;
-    // CTAs per SM from shared memory (registers allow two by the launch
-    // bounds); the occupancy query under-reports this kernel's.
-    int per_sm = smem_sm / (kSmem + reserved);
-    per_sm = per_sm < 1 ? 1 : (per_sm > 2 ? 2 : per_sm);
-    const int slots = sms * per_sm;
-    // Split each band's rows into chunks so that the items about fill the GPU
-    // once, keeping at least four rows per chunk (two halo rows per chunk).
-    p.bands = (p.w + kTileM - 1) / kTileM;
-    const long long strips = (long long)p.n * p.bands;
-    long long rpc = (strips * p.h + slots - 1) / slots;
-    if (rpc < 4) rpc = 4;
-    if (rpc > p.h) rpc = p.h;
-    p.rows_per_chunk = (int)rpc;
-    p.chunks = (p.h + p.rows_per_chunk - 1) / p.rows_per_chunk;
-    const long long items = strips * p.chunks;
-    if (items > 0x7fffffffLL) return cudaErrorInvalidValue;
-    p.items = (int)items;
-    const int grid = p.items < slots ? p.items : slots;
-    kern<<<grid, kThreadsTc, kSmem, s>>>(map, p);
+    if (!tensor_map_encoder()) return cudaErrorNotSupported;
+    if (!encode_rows_map(&map, in, CIN, p.n, p.h, p.w, kSlab)) return cudaErrorInvalidValue;
+    int slots = 0;
+    cudaError_t e = cta_slots(kSmem, &slots);
+    if (e != cudaSuccess) return e;
+    ItemPlan pl;
+    if (!plan_items(p.n, p.h, p.w, slots, pl)) return cudaErrorInvalidValue;
+    p.bands = pl.bands;
+    p.rows_per_chunk = pl.rows_per_chunk;
+    p.chunks = pl.chunks;
+    p.items = pl.items;
+    kern<<<pl.grid, kThreadsTc, kSmem, s>>>(map, p);
     return cudaGetLastError();
 }
 
@@ -705,38 +731,6 @@ __global__ void __launch_bounds__(kThreadsTc, 2)
     }
 }
 
-// Rows map over an NHWC BF16 tensor (channels, x, row, image), box of `box_px`
-// pixels, swizzled by a pixel's bytes (C = 16, 32 or 64).
-bool encode_rows_map(CUtensorMap *map, const void *base, int C, int n, int h, int w, int box_px) {
-    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
-    if (!encode) return false;
-    const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
-    const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)w * C * 2, (cuuint64_t)h * w * C * 2};
-    const cuuint32_t box[4] = {(cuuint32_t)C, (cuuint32_t)box_px, 1, 1};
-    const cuuint32_t estr[4] = {1, 1, 1, 1};
-    const CUtensorMapSwizzle swz =
-        C == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : (C == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B);
-    return encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(base), dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
-// CTA slots of a kernel with `smem` bytes of shared memory: two per SM at most.
-cudaError_t cta_slots(int smem, int *slots) {
-    int dev = 0, sms = 0, smem_sm = 0, reserved = 0;
-    cudaError_t e;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess)
-        return e;
-    if ((e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess)
-        return e;
-    int per_sm = smem_sm / (smem + reserved);
-    per_sm = per_sm < 1 ? 1 : (per_sm > 2 ? 2 : per_sm);
-    *slots = sms * per_sm;
-    return cudaSuccess;
-}
-
 template <int CIN, int COUT>
 cudaError_t launch_wgrad_tc(const __nv_bfloat16 *dout, const __nv_bfloat16 *in, WgradParams p, int max_parts,
                             int *parts, cudaStream_t s) {
@@ -758,19 +752,14 @@ cudaError_t launch_wgrad_tc(const __nv_bfloat16 *dout, const __nv_bfloat16 *in, 
     cudaError_t e = cta_slots(kSmem, &slots);
     if (e != cudaSuccess) return e;
     if (slots > max_parts) slots = max_parts;
-    p.bands = (p.w + kTileM - 1) / kTileM;
-    const long long strips = (long long)p.n * p.bands;
-    long long rpc = (strips * p.h + slots - 1) / slots;
-    if (rpc < 4) rpc = 4;
-    if (rpc > p.h) rpc = p.h;
-    p.rows_per_chunk = (int)rpc;
-    p.chunks = (p.h + p.rows_per_chunk - 1) / p.rows_per_chunk;
-    const long long items = strips * p.chunks;
-    if (items > 0x7fffffffLL || slots < 1) return cudaErrorInvalidValue;
-    p.items = (int)items;
-    const int grid = p.items < slots ? p.items : slots;
-    kern<<<grid, kThreadsTc, kSmem, s>>>(in_map, out_map, p);
-    *parts = grid;
+    ItemPlan pl;
+    if (!plan_items(p.n, p.h, p.w, slots, pl)) return cudaErrorInvalidValue;
+    p.bands = pl.bands;
+    p.rows_per_chunk = pl.rows_per_chunk;
+    p.chunks = pl.chunks;
+    p.items = pl.items;
+    kern<<<pl.grid, kThreadsTc, kSmem, s>>>(in_map, out_map, p);
+    *parts = pl.grid;
     return cudaGetLastError();
 }
 
