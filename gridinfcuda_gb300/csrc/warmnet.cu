@@ -54,13 +54,23 @@ struct Geo {
 constexpr int kChunk = 1024;
 
 // Bias gradient partials: sum over a chunk of pixels of g[p][c] (FP32).
-__global__ void k_bias_partials(const float *__restrict__ g, int npix, int C, float *__restrict__ partials) {
-    const int c = threadIdx.x;
-    if (c >= C) return;
+// 256 threads = 256 / C groups of C channels (C divides 256); group k sums
+// the chunk's pixels k, k + groups, ..., then the groups are added in order.
+__global__ void __launch_bounds__(256) k_bias_partials(const float *__restrict__ g, int npix, int C,
+                                                        float *__restrict__ partials) {
+    __shared__ float red[256];
+    const int groups = (int)blockDim.x / C, c = (int)threadIdx.x % C, grp = (int)threadIdx.x / C;
     const int pbeg = blockIdx.x * kChunk, pend = min(npix, pbeg + kChunk);
     float s = 0.f;
-    for (int p = pbeg; p < pend; ++p) s += g[(size_t)p * C + c];
-    partials[(size_t)blockIdx.x * C + c] = s;
+#pragma unroll 8
+    for (int p = pbeg + grp; p < pend; p += groups) s += g[(size_t)p * C + c];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    if ((int)threadIdx.x < C) {
+        float tot = 0.f;
+        for (int k = 0; k < groups; ++k) tot += red[k * C + threadIdx.x];
+        partials[(size_t)blockIdx.x * C + threadIdx.x] = tot;
+    }
 }
 
 // out[i] = sum over chunks k of partials[k][i], in chunk order; eight
@@ -113,11 +123,22 @@ void f32_to_bf16(const float *a, __nv_bfloat16 *b, size_t n, cudaStream_t s) {
 }
 
 // Loss = mean((y - t)^2) (per-block double partials), dy = 2 (y - t) / n.
+// Four values per thread and step (16-byte accesses) when the buffers are
+// 16-byte aligned; each four squares are summed in FP32 before the FP64
+// accumulation (a quarter of the FP64 additions).
 __global__ void k_mse(const float *__restrict__ y, const float *__restrict__ t, size_t n, float *__restrict__ dy,
                       double *__restrict__ partials) {
     double s = 0.0;
     const float scale = 2.f / (float)n;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t n4 = (((uintptr_t)y | (uintptr_t)t | (uintptr_t)dy) & 15) == 0 ? n / 4 : 0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x, t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (size_t i = t0; i < n4; i += stride) {
+        const float4 a = reinterpret_cast<const float4 *>(y)[i], b = reinterpret_cast<const float4 *>(t)[i];
+        const float d0 = a.x - b.x, d1 = a.y - b.y, d2 = a.z - b.z, d3 = a.w - b.w;
+        reinterpret_cast<float4 *>(dy)[i] = make_float4(scale * d0, scale * d1, scale * d2, scale * d3);
+        s += (double)(d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3);
+    }
+    for (size_t i = n4 * 4 + t0; i < n; i += stride) {
         const float d = y[i] - t[i];
         s += (double)d * d;
         dy[i] = scale * d;
@@ -132,12 +153,13 @@ __global__ void k_mse(const float *__restrict__ y, const float *__restrict__ t, 
     if (threadIdx.x == 0) partials[blockIdx.x] = red[0];
 }
 
+// One warp: lane l sums p[l], p[l + 32], ..., then the lanes combine in a
+// fixed shuffle order (lane 0's total is the result).
 __global__ void k_sum_double(const double *p, int n, double denom, float *out) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double s = 0.0;
-        for (int i = 0; i < n; ++i) s += p[i];
-        *out = (float)(s / denom);
-    }
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += 32) s += p[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) *out = (float)(s / denom);
 }
 
 // g = grad of a ReLU output times (activation > 0), FP32 and a BF16 copy.
@@ -389,7 +411,7 @@ ginf_status backward(ginf_warmnet *n, const float *target, Geo g, cudaStream_t s
     for (int l = 3; l >= 0; --l) {
         const int ci = n->cin[l], co = n->cout[l];
         // bias gradient
-        k_bias_partials<<<chunks, 128, 0, s>>>(gl, (int)pix, co, n->partials);
+        k_bias_partials<<<chunks, 256, 0, s>>>(gl, (int)pix, co, n->partials);
         k_reduce_partials<<<nblocks(co), kThreads, 0, s>>>(n->partials, chunks, co, n->grads + n->boff[l]);
         GINF_WCK(cudaGetLastError());
         // weight gradient

@@ -286,3 +286,20 @@ def test_tcgen05_convolutions_at_scale(ginf, L, shape):
     assert _rel(y.cpu().numpy(), want.cpu().numpy()) < 1e-4
     assert np.isfinite(loss1) and np.all(np.isfinite(g1))
     assert loss1 == loss2 and np.array_equal(g1, g2)
+
+
+def test_forward_in_place(ginf):
+    """ginf_warmnet_forward with y == x, which the header allows: the last
+    layer reads each residual element before the same thread writes it, so
+    the result equals a forward into a separate buffer, bit for bit."""
+    import torch
+    L = 32
+    params = REF.init_params(L, seed=5)
+    gen = torch.Generator(device="cuda").manual_seed(9)
+    x = torch.rand((2, 40, 150, L), device="cuda", generator=gen)
+    with ginf.WarmNet(L, 32) as net:
+        net.set_params(params)
+        y = net.forward(x)
+        z = x.clone()
+        ginf.check(ginf.lib().ginf_warmnet_forward(net.handle, z.data_ptr(), 2, 40, 150, z.data_ptr(), None))
+    assert torch.equal(y, z)
