@@ -78,13 +78,25 @@ __device__ void active_diagonals(const AlphaBetaParams &p, Shared &sh) {
         for (int w = threadIdx.x; w < (nd + 31) / 32; w += blockDim.x) sh.diag[w] = 0u;
     __syncthreads();
     int lo = 0x7fffffff, hi = -1;
-    for (size_t i = threadIdx.x; i < N; i += blockDim.x)
-        if (p.excess[i] && p.height[i] < NP2) {
+    // Four nodes per thread and step, their loads issued together.
+    for (size_t i0 = threadIdx.x; i0 < N; i0 += 4 * (size_t)blockDim.x) {
+        int32_t ev[4], hv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const size_t i = i0 + u * (size_t)blockDim.x;
+            ev[u] = i < N ? p.excess[i] : 0;
+            hv[u] = i < N ? p.height[i] : NP2;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (!(ev[u] && hv[u] < NP2)) continue;
+            const size_t i = i0 + u * (size_t)blockDim.x;
             const int k = (int)(i % W) + (int)(i / W);
             lo = min(lo, k);
             hi = max(hi, k);
             if (bits) atomicOr(&sh.diag[k >> 5], 1u << (k & 31));
         }
+    }
     if (hi >= 0) {
         atomicMin(&sh.kmin, lo);
         atomicMax(&sh.kmax, hi);
@@ -139,11 +151,21 @@ __device__ void sink_search(const AlphaBetaParams &p, int32_t *dist, Shared &sh)
     const int32_t *res = p.res;
     if (threadIdx.x == 0) sh.count = 0;
     __syncthreads();
-    for (size_t i = threadIdx.x; i < N; i += blockDim.x) {
-        dist[i] = 0;
-        if (res[kSink * N + i]) {
-            dist[i] = 1;
-            p.q0[atomicAdd(&sh.count, 1)] = (int32_t)i;
+    // Four nodes per thread and step, their loads issued together (the
+    // order of a frontier does not matter to the distances).
+    for (size_t i0 = threadIdx.x; i0 < N; i0 += 4 * (size_t)blockDim.x) {
+        int32_t rv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const size_t i = i0 + u * (size_t)blockDim.x;
+            rv[u] = i < N ? res[kSink * N + i] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const size_t i = i0 + u * (size_t)blockDim.x;
+            if (i >= N) break;
+            dist[i] = rv[u] ? 1 : 0;
+            if (rv[u]) p.q0[atomicAdd(&sh.count, 1)] = (int32_t)i;
         }
     }
     __syncthreads();
@@ -237,9 +259,19 @@ __global__ void __launch_bounds__(kThreadsAB, 1) k_alpha_beta(const AlphaBetaPar
                     if (sh.stop) break;
                     // graphCutGlobalRelabel (graphcut.cc:91-140).
                     sink_search(p, p.dist, sh);
-                    for (size_t i = threadIdx.x; i < N; i += blockDim.x) {
-                        const int32_t h = p.dist[i];
-                        ht[i] = h != 0 ? h : (ht[i] > NP2 ? ht[i] : NP2);
+                    for (size_t i0 = threadIdx.x; i0 < N; i0 += 4 * (size_t)blockDim.x) {
+                        int32_t dv[4], hv[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const size_t i = i0 + u * (size_t)blockDim.x;
+                            dv[u] = i < N ? p.dist[i] : 0;
+                            hv[u] = i < N ? ht[i] : 0;
+                        }
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const size_t i = i0 + u * (size_t)blockDim.x;
+                            if (i < N) ht[i] = dv[u] != 0 ? dv[u] : (hv[u] > NP2 ? hv[u] : NP2);
+                        }
                     }
                     __syncthreads();
                     const bool bits = W + H - 1 <= kDiagBits;
