@@ -131,13 +131,29 @@ __device__ int energy_i32(const AlphaBetaParams &p, const int32_t *f, Shared &sh
     const int W = p.W, H = p.H, L = p.L;
     const size_t N = (size_t)W * H;
     int acc = 0;
-    for (size_t i = threadIdx.x; i < N; i += blockDim.x) {
-        const int x = (int)(i % W), y = (int)(i / W);
-        if (x < 1 || y < 1 || x > W - 2 || y > H - 2) continue;
-        const int fl = f[i];
-        acc += p.D[i + N * fl];
-        acc += p.V[fl + (size_t)L * f[i - W]];
-        acc += p.V[fl + (size_t)L * f[i + 1]];
+    // Four nodes per thread and step: their labels, then their cost and
+    // table entries, each group of loads issued together (the int32 sum is
+    // order-independent).
+    for (size_t i0 = threadIdx.x; i0 < N; i0 += 4 * (size_t)blockDim.x) {
+        int fl[4], fn[4], fe[4];
+        bool in[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const size_t i = i0 + u * (size_t)blockDim.x;
+            const int x = i < N ? (int)(i % W) : 0, y = i < N ? (int)(i / W) : 0;
+            in[u] = i < N && x >= 1 && y >= 1 && x <= W - 2 && y <= H - 2;
+            fl[u] = in[u] ? f[i] : 0;
+            fn[u] = in[u] ? f[i - W] : 0;
+            fe[u] = in[u] ? f[i + 1] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (!in[u]) continue;
+            const size_t i = i0 + u * (size_t)blockDim.x;
+            acc += p.D[i + N * fl[u]];
+            acc += p.V[fl[u] + (size_t)L * fn[u]];
+            acc += p.V[fl[u] + (size_t)L * fe[u]];
+        }
     }
     return block_sum(acc, sh);
 }
@@ -248,7 +264,17 @@ __global__ void __launch_bounds__(kThreadsAB, 1) k_alpha_beta(const AlphaBetaPar
                 for (;;) {
                     // graphCutCountActive (graphcut.cc:75-88).
                     int act = 0;
-                    for (size_t i = threadIdx.x; i < N; i += blockDim.x) act += (ex[i] && ht[i] < NP2) ? 1 : 0;
+                    for (size_t i0 = threadIdx.x; i0 < N; i0 += 4 * (size_t)blockDim.x) {
+                        int32_t ev[4], hv[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const size_t i = i0 + u * (size_t)blockDim.x;
+                            ev[u] = i < N ? ex[i] : 0;
+                            hv[u] = i < N ? ht[i] : NP2;
+                        }
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) act += (ev[u] && hv[u] < NP2) ? 1 : 0;
+                    }
                     act = block_sum(act, sh);
                     if (act == 0) break;
                     if (threadIdx.x == 0 && global_timer_ns() - t0 > kAlphaBetaLimitNs) {
@@ -384,9 +410,17 @@ __global__ void __launch_bounds__(kThreadsAB, 1) k_alpha_beta(const AlphaBetaPar
                 // Nodes that reach the sink take alpha, the rest of the
                 // partition beta (graphcut.cc:253-263, 60-72).
                 sink_search(p, p.dist, sh);
-                for (size_t i = threadIdx.x; i < N; i += blockDim.x) {
-                    const int fl = nf[i];
-                    if (fl == alpha || fl == beta) nf[i] = p.dist[i] != 0 ? alpha : beta;
+                for (size_t i0 = threadIdx.x; i0 < N; i0 += 4 * (size_t)blockDim.x) {
+                    int fl[4], dv[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const size_t i = i0 + u * (size_t)blockDim.x;
+                        fl[u] = i < N ? nf[i] : -1;
+                        dv[u] = i < N ? p.dist[i] : 0;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (fl[u] == alpha || fl[u] == beta) nf[i0 + u * (size_t)blockDim.x] = dv[u] != 0 ? alpha : beta;
                 }
                 __syncthreads();
                 const int cost = energy_i32(p, nf, sh);
