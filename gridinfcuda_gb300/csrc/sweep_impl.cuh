@@ -608,7 +608,7 @@ __device__ void message_std_quad(const SweepParams &p, unsigned char *slot, int 
 // from m_0 = h.  A path of j steps that moves at k of them pays at least
 // s (1 + 3 + ... + (2k-1)) = s k^2, the first k steps, so in exact arithmetic
 // m_r(i) = min_{|k| <= r} h(i+k) + s k^2: the window's value, with the sums
-// rounded step by step instead of once (this store is judged against the
+// rounded step by step instead of once (this store is checked against the
 // FP64 run within a tolerance, not bit for bit).  Per output and pass one
 // packed addition for two outputs and one three-input minimum, against the
 // window's four pair minima, two three-input minima and the additions.  The

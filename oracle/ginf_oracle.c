@@ -181,7 +181,7 @@ void orc_minconv_brute_f64(int L, const double *f, const double *V, double *out)
 }
 
 /* ------------------------------------------------------------------------ */
-/* Standard min-sum BP in FP64 (the judge for the standard message rule, the */
+/* Standard min-sum BP in FP64 (the check for the standard message rule, the */
 /* FP16 message store and the quadratic model).  Same schedule as bp.cc:     */
 /* pyramid (bp.cc:100-117), coarse-to-fine copy (bp.cc:129-139), interior    */
 /* checkerboard half-sweeps (bp.cc:148-150).                                  */
