@@ -41,3 +41,23 @@ def test_parity_field_against_the_reference_result(orc):
     assert not bench.parity_vs_golden("plain", bad, orc.energy(P.D, P.V, bad))["ok"]
     assert not bench.parity_vs_golden("plain", lab, e * (1 + 1e-9))["ok"]
     assert isinstance(np.float64(par["energy"]), np.float64)
+
+
+def test_warmnet_roofline_arithmetic():
+    """The warm-start network's algorithmic bytes and FLOPs at 960x540x64, as
+    the warmnet bench line divides them by the measured time: x read as FP32
+    and written as BF16, each layer's BF16 input read and output written once
+    (the last layer's output FP32), the FP32 residual read once; 2 FLOPs per
+    multiply-add over 9 taps of every layer's channel pairs."""
+    import bench
+    pix = 960 * 540
+    nbytes, flops = bench.warmnet_bytes_flops(960, 540, 64)
+    want_bytes = (pix * 64 * (4 + 2)                          # x: FP32 read, BF16 write
+                  + pix * (64 + 32) * 2                        # layer 1: 64 in, 32 out (BF16)
+                  + 2 * pix * (32 + 32) * 2                    # layers 2, 3
+                  + pix * 32 * 2 + pix * 64 * 4                # layer 4: BF16 in, FP32 out
+                  + pix * 64 * 4)                              # residual x, FP32
+    assert nbytes == want_bytes
+    assert round(nbytes / 1e6, 1) == 729.9
+    assert flops == 2 * pix * 9 * (64 * 32 + 32 * 32 + 32 * 32 + 32 * 64)
+    assert round(flops / 1e9, 2) == 57.33
